@@ -1,0 +1,466 @@
+"""Benchmark of the GB300 virtual-pipe shallow-water step.
+
+Workload (the single-GPU configuration the headline metric is quoted on):
+one 4096 x 4096 FP32 grid, seeded PCG32 fBm terrain scaled to 0-40 m, initial
+depth max(0, 15 - b), closed walls, l = 1 m, A = 1 m^2, g = 9.81, dt = 0.02 s,
+damping 0.998 per step, one rain disk of radius 64 cells adding 0.01 m per
+step.  A benchmark "step" is a chain of `--chain` simulation steps (default
+200, so the default 50 timed steps make the configuration's 10,000 steps).
+
+Printed JSON line (rank 0):
+  value          Gcell-steps/s with the state resident in HBM (all ranks)
+  e2e            same metric through the C ABI with host buffers: per bench
+                 step, upload b/d/f from pinned host memory, the chain of steps,
+                 download d/f/v to pinned host memory
+  roofline       the step kernel: algorithmic bytes (52 B per cell-step for
+                 FP32 state) per launch / measured launch time, against the
+                 measured HBM copy bandwidth
+  cpu_baseline   the FP32 oracle (a CPU port of the reference shaders) on the
+                 host cores, bounded sample of the same grid; its state is
+                 compared with the GPU's for the same steps (full grid)
+  plain/blocked  the plain kernel (1 step per launch) and the temporally
+                 blocked kernel, both timed
+--impl reference times the CPU port of the reference's path on the host cores
+(the reference itself is an OpenGL program that cannot run on this machine).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W_DEFAULT = 4096
+BYTES_PER_CELL_STEP_F32 = 52.0   # read b 4 + d 4 + f 16, write d 4 + f 16 + v 8
+BYTES_PER_CELL_STEP_F16 = 36.0
+METRIC = "Gcell-steps/s and % of HBM peak, batched vs plain at same error; p50/p99 latency"
+L2_BYTES = 129e6
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--size", type=int, default=W_DEFAULT)
+    ap.add_argument("--chain", type=int, default=200, help="simulation steps per bench step")
+    ap.add_argument("--k", type=int, default=0, help="steps per launch for the headline (0: best)")
+    ap.add_argument("--flux", choices=["f32", "f16"], default="f32")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic_per_cell(k: int, flux: str):
+    """DRAM bytes per cell per launch of the step kernel from the committed ncu
+    summary (profiles/step_kernel_traffic.txt), or None."""
+    path = os.path.join(ROOT, "profiles", "step_kernel_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("#") or "=" not in line:
+            continue
+        kv = dict(tok.split("=", 1) for tok in line.split() if "=" in tok)
+        try:
+            if int(kv["k"]) == k and kv.get("flux", "f32") == flux:
+                return float(kv["dram_bytes_per_launch"]) / float(kv["cells"])
+        except (KeyError, ValueError):
+            continue
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        # nvidia-smi numbers GPUs physically; map through CUDA_VISIBLE_DEVICES
+        vis = [v.strip() for v in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if v.strip()]
+        self.index = vis[index] if index < len(vis) else str(index)
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        time.sleep(0.25)
+        self.rows = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            for line in out.strip().splitlines():
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) == 8:
+                    self.rows.append(parts)
+
+    def summary(self):
+        if not getattr(self, "rows", None):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[0]) for r in self.rows if num(r[0])]
+        smax = [num(r[1]) for r in self.rows if num(r[1])]
+        pw = [num(r[2]) for r in self.rows if num(r[2])]
+        loaded = [s for s in sm if smax and s > 0.5 * max(smax)] or sm
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if r[4 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(pw) if pw else None,
+                "samples": len(self.rows), "reasons": reasons}
+
+
+# ------------------------------------------------------------------ distributed
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def dist_init(ws, local):
+    import torch
+    import torch.distributed as dist
+    torch.cuda.set_device(local)
+    if ws > 1 and not dist.is_initialized():
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    return dist if ws > 1 else None
+
+
+def barrier(dist):
+    import torch
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ our arm
+
+def scene(tws, size):
+    p = tws.params_physical(0.02, 9.81, 1.0, 1.0, 0.998, tws.BOUNDARY_CLOSED)
+    rain = tws.rain_disks(2026, size, size, 64, 0.01, 1)
+    return p, rain
+
+
+def time_device(tws, torch, g, stream, k, chain, steps, warmup, dist):
+    """Timed region with the state resident in HBM.  Returns (seconds,
+    per-bench-step ms list, launches)."""
+    g.set_steps_per_launch(k)
+    for _ in range(warmup):
+        g.step(chain)
+    barrier(dist)
+    g.sync()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    L0 = tws.lib().tws_launch_count()
+    evs[0].record(stream)
+    for i in range(steps):
+        g.step(chain)
+        evs[i + 1].record(stream)
+    torch.cuda.synchronize()
+    launches = tws.lib().tws_launch_count() - L0
+    per = [evs[i].elapsed_time(evs[i + 1]) for i in range(steps)]
+    total = evs[0].elapsed_time(evs[steps]) / 1e3
+    g.sync()
+    return total, per, launches
+
+
+def run_ours(args):
+    import torch
+
+    import terrainwatersim_gb300 as tws
+
+    ws, rank, local = dist_env()
+    dist = dist_init(ws, local)
+    size, chain, steps, warmup = args.size, args.chain, args.steps, max(3, args.warmup)
+    flux = tws.FLUX_F16 if args.flux == "f16" else tws.FLUX_F32
+    bpc = BYTES_PER_CELL_STEP_F16 if args.flux == "f16" else BYTES_PER_CELL_STEP_F32
+    cells = size * size
+    peak, peak_kind = measured_peaks()
+    p, rain = scene(tws, size)
+    stream = torch.cuda.Stream()
+    g = tws.Grid(size, size, p, flux, stream=stream.cuda_stream)
+    g.generate_scene(2026, 40.0, 15.0)
+    g.set_sources(rain)
+    state_bytes = cells * (4 + 2 * 4 + 2 * (16 if flux == tws.FLUX_F32 else 8) + 8)
+
+    # plain and temporally blocked kernels, same workload
+    variants = {}
+    candidates = [1, 2, 3, 4] if args.k == 0 else sorted({1, args.k})
+    for k in candidates:
+        g.generate_scene(2026, 40.0, 15.0)
+        total, per, launches = time_device(tws, torch, g, stream, k, chain, steps, warmup, dist)
+        total = max_over_ranks(dist, total)
+        variants[k] = dict(seconds=total, per=per, launches=launches)
+    best_k = min(variants, key=lambda k: variants[k]["seconds"]) if args.k == 0 else args.k
+
+    # headline run of the chosen kernel with clocks sampled during it
+    g.generate_scene(2026, 40.0, 15.0)
+    with ClockSampler(local) as cs:
+        total, per, launches = time_device(tws, torch, g, stream, best_k, chain, steps, warmup, dist)
+    total = max_over_ranks(dist, total)
+    clocks = cs.summary()
+    cell_steps = float(cells) * chain * steps * ws
+    value = cell_steps / total / 1e9
+    launch_s = total / max(1, launches)  # only step kernels run in the timed region
+    cell_steps_per_launch = cells * best_k
+    achieved = bpc * cell_steps_per_launch / launch_s / 1e9
+    tpc = ncu_traffic_per_cell(best_k, args.flux)
+
+    # end to end through the C ABI with pinned host buffers
+    hb = torch.empty((size, size), dtype=torch.float32, pin_memory=True).numpy()
+    hd = torch.empty((size, size), dtype=torch.float32, pin_memory=True).numpy()
+    hf = torch.zeros((size, size, 4), dtype=torch.float32, pin_memory=True).numpy()
+    od = torch.empty((size, size), dtype=torch.float32, pin_memory=True).numpy()
+    of = torch.empty((size, size, 4), dtype=torch.float32, pin_memory=True).numpy()
+    ov = torch.empty((size, size, 2), dtype=torch.float32, pin_memory=True).numpy()
+    g.generate_scene(2026, 40.0, 15.0)
+    hb[...] = g.download_terrain()
+    g.download(out=(hd, None, None), flux=False, velocity=False)
+    g.set_steps_per_launch(best_k)
+    e2e_steps = max(3, steps // 2)
+    for _ in range(2):
+        g.upload(hb, hd, hf)
+        g.step(chain)
+        g.download(out=(od, of, ov))
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        g.upload(hb, hd, hf)
+        g.step(chain)
+        g.download(out=(od, of, ov))
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+    e2e_value = float(cells) * chain * e2e_steps * ws / e2e_s / 1e9
+
+    result = None
+    if rank == 0:
+        per_sorted = sorted(per)
+        result = {
+            "metric": METRIC,
+            "value": round(value, 3),
+            "unit": "Gcell-steps/s",
+            "n_gpus": ws,
+            "steps": steps,
+            "warmup": warmup,
+            "ms_per_step": round(total / steps * 1e3, 4),
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32" if flux == tws.FLUX_F32 else "f32 (f16 flux storage)",
+            "data": "synthetic: seeded PCG32 fBm terrain 0-40 m, fill 15 m, rain disk r=64",
+            "config": {
+                "workload": f"{size}x{size} FP32 virtual-pipe grid, closed walls, rain r=64, "
+                            f"{chain} simulation steps per bench step "
+                            f"({chain * steps} timed steps)",
+                "grid": [size, size],
+                "sim_steps_per_bench_step": chain,
+                "steps_per_launch": best_k,
+                "flux_storage": args.flux,
+                "l2": f"state {state_bytes / 1e6:.0f} MB > L2 {L2_BYTES / 1e6:.0f} MB, no flush",
+                "parallelism": "replicas (one whole grid per GPU)" if ws > 1 else "single grid",
+            },
+            "hbm_frac_of_measured": round(achieved / peak, 4),
+            "hbm_frac_of_8tbs_nominal": round(achieved / 8000.0, 4),
+            "p50_ms": round(per_sorted[len(per) // 2], 4),
+            "p99_ms": round(per_sorted[min(len(per) - 1, int(0.99 * len(per)))], 4),
+            "roofline": {
+                "bound": "hbm",
+                "achieved": round(achieved, 1),
+                "peak": peak,
+                "unit": "GB/s",
+                "frac": round(achieved / peak, 4),
+                "peak_kind": peak_kind,
+                "algorithmic_bytes_per_launch": bpc * cell_steps_per_launch,
+                "launch_us": round(launch_s * 1e6, 2),
+                "traffic": round(tpc * cells, 0) if tpc else None,
+                "dram_gbs": round(tpc * cells / launch_s / 1e9, 1) if tpc else None,
+                "kernel": f"step_kernel<K={best_k}>",
+            },
+            "variants": {
+                ("plain" if k == 1 else f"blocked_k{k}"): {
+                    "gcell_steps_per_s": round(cells * chain * steps * ws / v["seconds"] / 1e9, 3),
+                    "launch_us": round(v["seconds"] / max(1, v["launches"]) * 1e6, 2),
+                    "effective_gbs": round(bpc * cells * k / (v["seconds"] / max(1, v["launches"]))
+                                           / 1e9, 1),
+                } for k, v in variants.items()},
+            "e2e": {
+                "value": round(e2e_value, 3),
+                "unit": "Gcell-steps/s",
+                "h2d_bytes_per_step": int(hb.nbytes + hd.nbytes + hf.nbytes),
+                "d2h_bytes_per_step": int(od.nbytes + of.nbytes + ov.nbytes),
+                "steps": e2e_steps,
+            },
+            "gpu_launches": int(launches),
+            "clocks": clocks,
+        }
+        if ws == 1 and not args.no_cpu:
+            result["cpu_baseline"] = cpu_baseline_leg(tws, g, size, args.cpu_seconds)
+    g.close()
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return result
+
+
+def cpu_baseline_leg(tws, g, size, budget_s):
+    """The FP32 oracle on the host cores, bounded sample of the same grid; the
+    GPU's state after the same steps is compared with it on the full grid."""
+    from oracle import oracle as O
+
+    p, rain = scene(tws, size)
+    b, d = O.terrain(2026, size, size, 40.0, 15.0)
+    f = np.zeros((size, size, 4), np.float32)
+    v = np.zeros((size, size, 2), np.float32)
+    src = [(s[0], s[1], s[2], s[3], s[4]) for s in rain]
+    kf, ka, c = p.as_tuple()
+    threads = O.max_threads()
+    t1 = O.step_f32(b, d, f, v, kf, ka, c, O.BOUNDARY_CLOSED, src, nsteps=1, threads=threads)
+    n = int(max(1, min(400, budget_s / max(t1, 1e-6))))
+    tn = O.step_f32(b, d, f, v, kf, ka, c, O.BOUNDARY_CLOSED, src, nsteps=n, threads=threads)
+    total_steps = n + 1
+    # the GPU on the same steps
+    g.generate_scene(2026, 40.0, 15.0)
+    g.set_sources(rain)
+    g.step(total_steps)
+    gd, gf, gv = g.download()
+    err = float(np.abs(gd.astype(np.float64) - d).max())
+    rel = err / max(1e-30, float(np.abs(d).max()))
+    bitexact = bool(np.array_equal(gd.view(np.uint32), d.view(np.uint32))
+                    and np.array_equal(gf.view(np.uint32), f.view(np.uint32))
+                    and np.array_equal(gv.view(np.uint32), v.view(np.uint32)))
+    vg, vo = float(np.sum(gd, dtype=np.float64)), O.volume(d)
+    return {
+        "value": round(size * size * n / tn / 1e9, 4),
+        "unit": "Gcell-steps/s",
+        "cores": threads,
+        "kind": "port",
+        "sample": f"{size}x{size} grid, {n} steps timed (+1 warm-up step), FP32 oracle, "
+                  f"OpenMP {threads} threads; GPU state after the same {total_steps} steps "
+                  "compared on the full grid",
+        "seconds": round(tn, 3),
+        "parity": {"steps": total_steps, "bitexact": bitexact, "max_abs_depth_err": err,
+                   "rel_max_depth_err": rel,
+                   "rel_volume_diff": abs(vg - vo) / max(1e-30, abs(vo))},
+    }
+
+
+# ------------------------------------------------------------------ reference arm
+
+def run_reference(args):
+    """The reference's path on the host cores: the CPU port of its shaders
+    (the reference itself is an OpenGL/Win32 program that cannot run here).
+    Each bench step advances the same 4096^2 grid by `ref_chain` steps."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return None
+    from oracle import oracle as O
+
+    size = args.size
+    ref_chain = 5
+    kf, ka, c = (np.float32(x) for x in O.params_physical(0.02, 9.81, 1.0, 1.0, 0.998))
+    (cx, cy), = O.rain_centers(2026, size, size, 64, 1)
+    src = [(O.SOURCE_DISK, cx, cy, 64, 0.01)]
+    b, d = O.terrain(2026, size, size, 40.0, 15.0)
+    f = np.zeros((size, size, 4), np.float32)
+    v = np.zeros((size, size, 2), np.float32)
+    threads = O.max_threads()
+    warmup = max(3, args.warmup)
+    for _ in range(warmup):
+        O.step_f32(b, d, f, v, kf, ka, c, O.BOUNDARY_CLOSED, src, nsteps=ref_chain, threads=threads)
+    per = []
+    for _ in range(args.steps):
+        per.append(O.step_f32(b, d, f, v, kf, ka, c, O.BOUNDARY_CLOSED, src, nsteps=ref_chain,
+                              threads=threads))
+    total = sum(per)
+    value = size * size * ref_chain * args.steps / total / 1e9
+    return {
+        "metric": METRIC,
+        "impl": "reference",
+        "value": round(value, 4),
+        "unit": "Gcell-steps/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": warmup,
+        "ms_per_step": round(total / args.steps * 1e3, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic: seeded PCG32 fBm terrain 0-40 m, fill 15 m, rain disk r=64",
+        "config": {
+            "workload": f"{size}x{size} FP32 virtual-pipe grid, closed walls, rain r=64, "
+                        f"{ref_chain} simulation steps per bench step (bounded CPU sample)",
+            "grid": [size, size],
+            "sim_steps_per_bench_step": ref_chain,
+            "parallelism": "host cores (OpenMP)",
+        },
+        "cpu_baseline": {
+            "value": round(value, 4), "unit": "Gcell-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{size}x{size} grid, {ref_chain} steps per bench step, FP32 CPU port of "
+                      "flowUpdate.comp + flowApply.comp (the reference runs them through OpenGL, "
+                      "which this machine does not have)",
+        },
+        "e2e": {"value": round(value, 4), "unit": "Gcell-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "p50_ms": round(sorted(per)[len(per) // 2] * 1e3, 3),
+        "p99_ms": round(sorted(per)[min(len(per) - 1, int(0.99 * len(per)))] * 1e3, 3),
+    }
+
+
+def main():
+    args = parse()
+    res = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if res is not None:
+        print(json.dumps(res), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,201 @@
+/* tws.h -- C ABI of the GB300 virtual-pipe shallow-water step.
+ *
+ * This is the drop-in boundary for the simulation half of terrainwatersim's
+ * `Terrain` class (terrainwatersim/source/scene/Terrain.h:15-153).  The
+ * reference keeps its state in three OpenGL textures and advances it with two
+ * compute-shader dispatches per step; this library keeps the same state in
+ * device buffers on one GPU and advances it with hand-written sm_103a kernels.
+ *
+ * Conventions
+ *   - Every call returns an int status: TWS_OK (0) or a negative TWS_ERR_*.
+ *     tws_error_string() names a code; tws_last_error() gives the message of
+ *     the last failure on a grid.  No C++ exception crosses this boundary.
+ *   - Host arrays are row-major, tightly packed, `width` floats per row.
+ *     Flux is 4 floats per cell in the reference's channel order
+ *     (+x, -x, +y, -y) = (.x, .y, .z, .w) of the Flow texture
+ *     (flowUpdate.comp:44-47); velocity ("flow map") is 2 floats per cell
+ *     (flowApply.comp:45-46).
+ *   - Calls on one grid are enqueued on that grid's CUDA stream and are
+ *     asynchronous unless stated.  One grid must not be used from two host
+ *     threads at once; distinct grids are independent.
+ *   - There is no CPU fallback: without a usable sm_103a device, tws_create
+ *     fails with TWS_ERR_CUDA.
+ */
+#ifndef TWS_H_
+#define TWS_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TWS_API __attribute__((visibility("default")))
+
+/* ---- status codes ---------------------------------------------------- */
+#define TWS_OK 0
+#define TWS_ERR_INVALID -1     /* bad argument (size, pointer, enum)        */
+#define TWS_ERR_CUDA -2        /* a CUDA runtime/driver call failed         */
+#define TWS_ERR_OOM -3         /* device allocation failed                  */
+#define TWS_ERR_TIMEOUT -4     /* a device-side bounded wait gave up        */
+#define TWS_ERR_UNSUPPORTED -5 /* option not built into this library        */
+#define TWS_ERR_BUSY -6        /* admission refused (serving loop)          */
+
+/* ---- enums ------------------------------------------------------------ */
+#define TWS_BOUNDARY_CLOSED 0 /* zero flux across the grid border          */
+#define TWS_BOUNDARY_OPEN 1   /* reference semantics: off-grid cells read  */
+                              /* as zero, water drains off the edge        */
+                              /* (GL imageLoad out of range, flowUpdate.comp:18,29-32) */
+#define TWS_FLUX_F32 0        /* flux stored as 4 x float per cell          */
+#define TWS_FLUX_F16 1        /* flux stored as 4 x half per cell, times a  */
+                              /* per-grid power-of-two scale               */
+#define TWS_SOURCE_DISK 0     /* uniform disk: +rate metres per step inside */
+#define TWS_SOURCE_BRUSH 1    /* reference radial brush, waterBrush.comp:26-28 */
+
+#define TWS_MAX_SOURCES 8
+
+/* ---- parameters --------------------------------------------------------
+ * The three per-step constants of the reference's SimulationParameters
+ * uniform block (terrainwatersim/shader/simulationCommon.glsl:1-13).       */
+typedef struct tws_sim_params {
+  float flow_friction_per_step;      /* Kf, FlowFriction_perStep            */
+  float water_acceleration_per_step; /* Ka, WaterAcceleration_perStep       */
+  float cell_area_inv_time_scaled;   /* C,  CellAreaInv_timeScaled          */
+  float cell_area;                   /* l*l, scales tws_volume               */
+  int boundary;                      /* TWS_BOUNDARY_*                       */
+} tws_sim_params;
+
+/* Physical form: Kf = damping_per_step, Ka = dt*g*A/l, C = dt/l^2 (the
+ * formulas stated in simulationCommon.glsl:5-11), evaluated in double and
+ * rounded to float once. */
+TWS_API int tws_params_physical(double dt, double gravity, double pipe_area, double cell_size,
+                                double damping_per_step, int boundary, tws_sim_params* out);
+
+/* Reference form: the derivations of Terrain::SetSimulationStepsPerSecond,
+ * SetFlowDamping and SetFlowAcceleration (Terrain.cpp:175-198):
+ * Kf = pow(damping, step), Ka = step*acceleration*cellDistance,
+ * C = step/cellDistance^2, with step = 1/steps_per_second and
+ * cellDistance = grid_world_size/grid_resolution. */
+TWS_API int tws_params_reference(float steps_per_second, float flow_damping,
+                                 float flow_acceleration, float grid_world_size,
+                                 unsigned grid_resolution, int boundary, tws_sim_params* out);
+
+/* A water source.  DISK (the benchmark's rain): every cell whose integer
+ * offset (x-cx, y-cy) satisfies dx*dx+dy*dy <= radius*radius gains `rate`
+ * metres (cx, cy, radius are whole cells).  BRUSH (the reference's brush,
+ * waterBrush.comp:26-28): d += saturate(1 - |(cx,cy)-(x,y)|^2 / radius) * rate,
+ * where radius holds BrushSizeSq and rate BrushIntensity. */
+typedef struct tws_source {
+  int kind;
+  float cx, cy;
+  float radius;
+  float rate;
+} tws_source;
+
+typedef struct tws_grid tws_grid; /* opaque */
+
+/* Device view of a grid's state, valid until the next tws_step or
+ * tws_destroy (the step ping-pongs depth and flux).  Rows are `pitch`
+ * elements apart. */
+typedef struct tws_buffers {
+  const float* terrain;  /* b, float per cell                                */
+  const float* depth;    /* d, float per cell                                */
+  const void* flux;      /* 4 x float (F32) or 4 x half (F16) per cell       */
+  const float* velocity; /* 2 x float per cell (flow map, last step)         */
+  int width, height, pitch;
+  int flux_storage;      /* TWS_FLUX_*                                       */
+  float flux_scale;      /* F16: stored = flux * flux_scale (power of two)  */
+} tws_buffers;
+
+/* ---- lifecycle -----------------------------------------------------------
+ * Replaces Terrain::Terrain + CreateHeightmapFromNoiseAndResetSim's texture
+ * allocation (Terrain.cpp:21-132, 200-238).  `stream` is a cudaStream_t
+ * (NULL: the library creates one).  State starts as b = d = f = v = 0. */
+TWS_API int tws_create(int width, int height, const tws_sim_params* params, int flux_storage,
+                       void* stream, tws_grid** out);
+/* Replaces Terrain::~Terrain (Terrain.cpp:134-148). */
+TWS_API int tws_destroy(tws_grid* grid);
+
+/* Reset from host arrays: terrain (required), depth (NULL -> 0), flux
+ * (NULL -> 0); velocity is cleared.  Replaces the uploads of
+ * CreateHeightmapFromNoiseAndResetSim (Terrain.cpp:223, 230-234).
+ * Synchronous with respect to the host arrays (they may be reused on return). */
+TWS_API int tws_upload(tws_grid* grid, const float* terrain, const float* depth,
+                       const float* flux);
+/* Same, from tightly packed device arrays. */
+TWS_API int tws_upload_device(tws_grid* grid, const float* terrain, const float* depth,
+                              const float* flux);
+
+/* Reset to the synthetic benchmark scene, generated on the device: seeded
+ * PCG32 value-noise fBm terrain scaled to [0, height_scale), depth
+ * max(0, fill - b), flux and velocity zero.  Stands in for
+ * CreateHeightmapFromNoiseAndResetSim (Terrain.cpp:200-238), whose own noise
+ * generator is not the benchmark's. */
+TWS_API int tws_generate_scene(tws_grid* grid, uint64_t seed, float height_scale, float fill);
+
+/* Rain disks of the synthetic benchmark scene: `count` DISK sources of the
+ * given radius and rate, centres drawn from the PCG32 stream
+ * (seed, 1000 + k): cx = r + u0 % (W - 2r), cy = r + u1 % (H - 2r) (grid
+ * centre if the disk does not fit).  Host-only; no counterpart in the
+ * reference, whose water source is the interactive brush. */
+TWS_API int tws_scene_rain_disks(uint64_t seed, int width, int height, int radius, float rate,
+                                 int count, tws_source* out);
+
+/* Replaces the SimulationParameters setters (Terrain.cpp:175-198). */
+TWS_API int tws_set_params(tws_grid* grid, const tws_sim_params* params);
+
+/* Per-step sources, applied at the start of every step inside the step
+ * kernel (n <= TWS_MAX_SOURCES; n = 0 clears). */
+TWS_API int tws_set_sources(tws_grid* grid, const tws_source* sources, int n);
+
+/* One-shot source applied now, before the next step: replaces
+ * Terrain::ApplyRadialWaterBrush's dispatch (Terrain.cpp:150-168). */
+TWS_API int tws_apply_source(tws_grid* grid, const tws_source* source);
+
+/* Steps per launch of the fused kernel (temporal blocking depth): 1 (plain),
+ * 2, 3 or 4.  0 selects the library's choice for this grid size.  Results do
+ * not depend on it (bit-identical). */
+TWS_API int tws_set_steps_per_launch(tws_grid* grid, int steps_per_launch);
+
+/* Advance `nsteps` steps: per step, sources, then the outflow update with
+ * non-negativity scaling (flowUpdate.comp:12-63), then the depth update and
+ * flow vector (flowApply.comp:13-53), fused.  Replaces the dispatch loop of
+ * Terrain::PerformSimulationStep (Terrain.cpp:253-265).  Asynchronous. */
+TWS_API int tws_step(tws_grid* grid, int nsteps);
+
+/* Total water volume sum(d) * cell_area, accumulated in FP64 on the device
+ * (no counterpart in the reference).  Synchronous; deterministic. */
+TWS_API int tws_volume(tws_grid* grid, double* out);
+
+/* Copy state to host arrays (each may be NULL).  Flux is returned as 4 floats
+ * per cell whatever the storage.  Synchronous. */
+TWS_API int tws_download(tws_grid* grid, float* depth, float* flux, float* velocity);
+/* Copy terrain to a host array.  Synchronous. */
+TWS_API int tws_download_terrain(tws_grid* grid, float* terrain);
+
+/* Device pointers (replaces binding the textures for drawing,
+ * Terrain.cpp:288, 323-330). */
+TWS_API int tws_get_buffers(tws_grid* grid, tws_buffers* out);
+
+/* Block the host until the grid's queued work is done; reports a device-side
+ * error (TWS_ERR_TIMEOUT) raised by any kernel of this grid. */
+TWS_API int tws_sync(tws_grid* grid);
+
+/* The grid's CUDA stream (cudaStream_t). */
+TWS_API void* tws_stream(tws_grid* grid);
+
+TWS_API const char* tws_error_string(int code);
+TWS_API const char* tws_last_error(tws_grid* grid);
+
+/* Number of kernels this library has launched in this process (for
+ * benchmarks that report their launch count). */
+TWS_API uint64_t tws_launch_count(void);
+
+/* Library version string. */
+TWS_API const char* tws_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TWS_H_ */

@@ -1,0 +1,428 @@
+// tws_oracle.cpp -- TEST INFRASTRUCTURE, NOT PART OF THE PRODUCT.
+//
+// CPU restatement of terrainwatersim's virtual-pipe shallow-water step, used only
+// as the correctness checker (tests/, the smoke check) and as the timed CPU
+// baseline (bench.py).  The product path (libtws.so) never links, loads or calls
+// this file.
+//
+// It follows the reference's arithmetic in the same operation order:
+//   * flux update   terrainwatersim/shader/flowUpdate.comp:34-62
+//   * depth / flow  terrainwatersim/shader/flowApply.comp:32-52
+//   * parameters    terrainwatersim/shader/simulationCommon.glsl:1-13,
+//                   terrainwatersim/source/scene/Terrain.cpp:175-198
+//   * brush source  terrainwatersim/shader/waterBrush.comp:26-28 (+ helper.glsl:68)
+//   * step order    terrainwatersim/source/scene/Terrain.cpp:253-265 (all fluxes,
+//                   then all depths; the brush runs before the step,
+//                   terrainwatersim/source/scene/Scene.cpp:354-363)
+// GLSL semantics kept: an out-of-range imageLoad reads zero (boundary OPEN),
+// max(x, y) = (x < y) ? y : x, left-to-right '+' chains, vec4 ops per component.
+// The closed-wall boundary (zero flux across the border) is this project's
+// addition for the benchmark configurations; it differs from OPEN only in the
+// outflow component that points off the grid, which it forces to zero.
+//
+// Pinning: the FP32 OPEN-boundary path is checked bit-for-bit against the
+// reference's own shader source executed on the CPU (oracle/ref_glsl, built by
+// oracle/Makefile into oracle/_ref) and against the fixtures in tests/golden.
+//
+// Built twice from one template: float (the FP32 transcription) and double (the
+// FP64 oracle).  Must be compiled with -ffp-contract=off (no FMA contraction).
+//
+// Also holds the synthetic scene generator (seeded PCG32 value-noise fBm) that
+// the product library restates on the host and on the device; tests check the
+// two agree bit for bit.
+
+#include <chrono>
+#include <cmath>
+#include <cstddef>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+extern "C" {
+
+// Source term applied at the start of every step (before the flux update).
+//   kind 0 = DISK  : every cell with (x-cx)^2 + (y-cy)^2 <= r^2 (integer cells)
+//                    gains `rate` metres of water.
+//   kind 1 = BRUSH : the reference's radial brush, waterBrush.comp:26-28,
+//                    d += saturate(1 - |(cx,cy) - (x,y)|^2 / size_sq) * rate.
+typedef struct tws_oracle_source {
+  int kind;
+  int pad_;
+  double cx, cy;
+  double radius;   // DISK: radius in cells (integer valued); BRUSH: BrushSizeSq
+  double rate;     // DISK: metres per step; BRUSH: BrushIntensity
+} tws_oracle_source;
+
+}  // extern "C"
+
+namespace {
+
+template <class T>
+struct F4 {
+  T x, y, z, w;
+};
+template <class T>
+struct F2 {
+  T x, y;
+};
+
+// GLSL max(0, v): returns v if 0 < v, else 0 (flowUpdate.comp:54, flowApply.comp:41).
+template <class T>
+inline T glsl_max0(T v) {
+  return (T(0) < v) ? v : T(0);
+}
+
+// GLSL clamp(v, 0, 1) = min(max(v, 0), 1) (helper.glsl:68 `saturate`).
+template <class T>
+inline T glsl_saturate(T v) {
+  T m = (v < T(0)) ? T(0) : v;   // max(v, 0) = (v < 0) ? 0 : v
+  return (T(1) < m) ? T(1) : m;  // min(m, 1) = (1 < m) ? 1 : m
+}
+
+template <class T>
+struct Params {
+  T kf;  // FlowFriction_perStep
+  T ka;  // WaterAcceleration_perStep
+  T c;   // CellAreaInv_timeScaled
+  int closed;
+  T flux_scale;  // > 0: flux is stored as IEEE half of flux * flux_scale (FP32 only)
+};
+
+// The value an FP16-stored flux reads back as: half(min(v * scale, 65504)),
+// rounded to nearest even, times 1/scale (scale is a power of two).
+template <class T>
+inline T quantize_half(T v, T scale) {
+  T s = v * scale;
+  s = (s < T(65504)) ? s : T(65504);
+  const _Float16 h = (_Float16)(float)s;
+  return (T)((float)h) * (T(1) / scale);
+}
+
+inline int num_threads(int requested) {
+#ifdef _OPENMP
+  return requested > 0 ? requested : omp_get_max_threads();
+#else
+  (void)requested;
+  return 1;
+#endif
+}
+
+// Source term.  DISK follows the benchmark's uniform rain disk; BRUSH follows
+// waterBrush.comp:26-28: toBrush = BrushPos - gridPosition; q = dot / S;
+// d += saturate(1 - q) * I.  Cells where the increment is zero are left as
+// they are (d + 0 == d for every d >= +0, the only depths the step produces).
+template <class T>
+void apply_sources(int W, int H, T* d, const tws_oracle_source* src, int nsrc, int nth) {
+  for (int k = 0; k < nsrc; ++k) {
+    const tws_oracle_source& s = src[k];
+    if (s.kind == 0) {
+      const int cx = (int)s.cx, cy = (int)s.cy, r = (int)s.radius;
+      const long long r2 = (long long)r * r;
+      const T rate = (T)s.rate;
+      const int y0 = cy - r < 0 ? 0 : cy - r, y1 = cy + r >= H ? H - 1 : cy + r;
+      const int x0 = cx - r < 0 ? 0 : cx - r, x1 = cx + r >= W ? W - 1 : cx + r;
+#pragma omp parallel for num_threads(nth) schedule(static)
+      for (int y = y0; y <= y1; ++y)
+        for (int x = x0; x <= x1; ++x) {
+          const long long dx = x - cx, dy = y - cy;
+          if (dx * dx + dy * dy <= r2) d[(size_t)y * W + x] = d[(size_t)y * W + x] + rate;
+        }
+    } else {
+      const T bx = (T)s.cx, by = (T)s.cy, S = (T)s.radius, I = (T)s.rate;
+#pragma omp parallel for num_threads(nth) schedule(static)
+      for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+          const T tx = bx - (T)x, ty = by - (T)y;
+          const T q = (tx * tx + ty * ty) / S;
+          const T inc = glsl_saturate(T(1) - q) * I;
+          if (inc != T(0)) d[(size_t)y * W + x] = d[(size_t)y * W + x] + inc;
+        }
+    }
+  }
+}
+
+// flowUpdate.comp:34-62, in place on f (the shader reads and writes only its own
+// cell's flux, so in-place is exact).  Channel order: x = +x, y = -x, z = +y, w = -y.
+template <class T>
+void flux_update(int W, int H, const Params<T>& p, const T* b, const T* d, F4<T>* f, int nth) {
+#pragma omp parallel for num_threads(nth) schedule(static)
+  for (int y = 0; y < H; ++y) {
+    const size_t row = (size_t)y * W;
+    for (int x = 0; x < W; ++x) {
+      const size_t i = row + x;
+      const T hc = d[i] + b[i];                                   // :34
+      const T hx1 = (x + 1 < W) ? d[i + 1] + b[i + 1] : T(0);    // :37-40, OOB reads 0
+      const T hx0 = (x > 0) ? d[i - 1] + b[i - 1] : T(0);
+      const T hy1 = (y + 1 < H) ? d[i + W] + b[i + W] : T(0);
+      const T hy0 = (y > 0) ? d[i - W] + b[i - W] : T(0);
+      const T ex1 = hc - hx1, ex0 = hc - hx0, ey1 = hc - hy1, ey0 = hc - hy0;  // :44-47
+      const F4<T> fo = f[i];                                                   // :50
+      F4<T> nf;                                                                // :53
+      nf.x = fo.x * p.kf + ex1 * p.ka;
+      nf.y = fo.y * p.kf + ex0 * p.ka;
+      nf.z = fo.z * p.kf + ey1 * p.ka;
+      nf.w = fo.w * p.kf + ey0 * p.ka;
+      nf.x = glsl_max0(nf.x);  // :54
+      nf.y = glsl_max0(nf.y);
+      nf.z = glsl_max0(nf.z);
+      nf.w = glsl_max0(nf.w);
+      if (p.closed) {  // zero flux across the outer wall
+        if (x + 1 >= W) nf.x = T(0);
+        if (x == 0) nf.y = T(0);
+        if (y + 1 >= H) nf.z = T(0);
+        if (y == 0) nf.w = T(0);
+      }
+      const T total = (((nf.x + nf.y) + nf.z) + nf.w) * p.c;  // :57
+      const T dc = d[i];
+      if (total > dc) {  // :58-59
+        const T s = dc / total;
+        nf.x = nf.x * s;
+        nf.y = nf.y * s;
+        nf.z = nf.z * s;
+        nf.w = nf.w * s;
+      }
+      if (p.flux_scale > T(0)) {  // FP16 flux storage: the apply uses the stored value
+        nf.x = quantize_half(nf.x, p.flux_scale);
+        nf.y = quantize_half(nf.y, p.flux_scale);
+        nf.z = quantize_half(nf.z, p.flux_scale);
+        nf.w = quantize_half(nf.w, p.flux_scale);
+      }
+      f[i] = nf;  // :62
+    }
+  }
+}
+
+// flowApply.comp:32-52, in place on d (reads only its own cell's depth).
+template <class T>
+void flow_apply(int W, int H, const Params<T>& p, T* d, const F4<T>* f, F2<T>* v, int nth) {
+#pragma omp parallel for num_threads(nth) schedule(static)
+  for (int y = 0; y < H; ++y) {
+    const size_t row = (size_t)y * W;
+    for (int x = 0; x < W; ++x) {
+      const size_t i = row + x;
+      const F4<T> fo = f[i];
+      const T X1 = (x + 1 < W) ? f[i + 1].y : T(0);  // :32-35, OOB reads 0
+      const T X0 = (x > 0) ? f[i - 1].x : T(0);
+      const T Y1 = (y + 1 < H) ? f[i + W].w : T(0);
+      const T Y0 = (y > 0) ? f[i - W].z : T(0);
+      const T in = ((X1 + X0) + Y1) + Y0;                // :38
+      const T out = ((fo.x + fo.y) + fo.z) + fo.w;       // :39
+      d[i] = glsl_max0(d[i] + (in - out) * p.c);         // :41
+      if (v) {
+        v[i].x = (X1 - fo.x) - (X0 - fo.y);  // :45
+        v[i].y = (Y1 - fo.z) - (Y0 - fo.w);  // :46
+      }
+    }
+  }
+}
+
+template <class T>
+void run_steps(int W, int H, const Params<T>& p, const T* b, T* d, F4<T>* f, F2<T>* v,
+               const tws_oracle_source* src, int nsrc, int nsteps, int nth) {
+  for (int s = 0; s < nsteps; ++s) {
+    apply_sources(W, H, d, src, nsrc, nth);
+    flux_update(W, H, p, b, d, f, nth);
+    flow_apply(W, H, p, d, f, v, nth);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Synthetic scene generator (the benchmark's terrain, not the reference's
+// NoiseGenerator): seeded PCG32 value noise, lattice spacing 64 cells, 6
+// octaves (spacing halves, amplitude halves), smoothstep-bilinear
+// interpolation, normalised by the amplitude sum 1.96875 and scaled.
+// PCG32 is O'Neill's XSH-RR 64/32 generator (pcg-random.org, "pcg32").
+
+const uint64_t kPcgMult = 6364136223846793005ULL;
+
+struct Pcg32 {
+  uint64_t state, inc;
+  void seed(uint64_t initstate, uint64_t initseq) {
+    state = 0u;
+    inc = (initseq << 1u) | 1u;
+    next();
+    state += initstate;
+    next();
+  }
+  uint32_t next() {
+    const uint64_t old = state;
+    state = old * kPcgMult + inc;
+    const uint32_t xorshifted = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+    const uint32_t rot = (uint32_t)(old >> 59u);
+    return (xorshifted >> rot) | (xorshifted << ((0u - rot) & 31u));
+  }
+  // Jump ahead by delta steps (Brown, "Random number generation with
+  // arbitrary strides", 1994): the LCG composed with itself.
+  void advance(uint64_t delta) {
+    uint64_t cur_mult = kPcgMult, cur_plus = inc, acc_mult = 1u, acc_plus = 0u;
+    while (delta > 0) {
+      if (delta & 1u) {
+        acc_mult *= cur_mult;
+        acc_plus = acc_plus * cur_mult + cur_plus;
+      }
+      cur_plus = (cur_mult + 1u) * cur_plus;
+      cur_mult *= cur_mult;
+      delta >>= 1u;
+    }
+    state = acc_mult * state + acc_plus;
+  }
+};
+
+inline float u01(uint32_t u) { return (float)(u >> 8) * (1.0f / 16777216.0f); }
+
+inline float smooth01(float t) {
+  const float a = t * t;
+  const float c = 3.0f - 2.0f * t;
+  return a * c;
+}
+inline float lerpf(float a, float b, float t) { return a + (b - a) * t; }
+
+}  // namespace
+
+extern "C" {
+
+// Version tag of the scene generator definition; the product library reports
+// the same number.
+int tws_oracle_scene_version(void) { return 1; }
+
+// Lattice value for octave o at lattice point (i, j): output number j*Lx + i of
+// the PCG32 stream (seed, o + 1), mapped to [0, 1) with 24 bits.
+void tws_oracle_terrain(uint64_t seed, int W, int H, float height_scale, float fill, float* b,
+                        float* d) {
+  const int kOct = 6;
+  std::vector<std::vector<float>> lat(kOct);
+  std::vector<int> lx(kOct);
+  for (int o = 0; o < kOct; ++o) {
+    const int s = 64 >> o;
+    const int Lx = W / s + 2, Ly = H / s + 2;
+    lx[o] = Lx;
+    lat[o].resize((size_t)Lx * Ly);
+    Pcg32 g;
+    g.seed(seed, (uint64_t)o + 1u);
+    for (size_t k = 0; k < lat[o].size(); ++k) lat[o][k] = u01(g.next());
+  }
+#pragma omp parallel for schedule(static)
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      float acc = 0.0f, amp = 1.0f;
+      for (int o = 0; o < kOct; ++o) {
+        const int s = 64 >> o;
+        const float inv = 1.0f / (float)s;
+        const int i = x / s, j = y / s;
+        const float sx = smooth01((float)(x % s) * inv);
+        const float sy = smooth01((float)(y % s) * inv);
+        const float* L = lat[o].data();
+        const int Lx = lx[o];
+        const float v00 = L[(size_t)j * Lx + i], v10 = L[(size_t)j * Lx + i + 1];
+        const float v01 = L[(size_t)(j + 1) * Lx + i], v11 = L[(size_t)(j + 1) * Lx + i + 1];
+        const float v = lerpf(lerpf(v00, v10, sx), lerpf(v01, v11, sx), sy);
+        acc = acc + amp * v;
+        amp = amp * 0.5f;
+      }
+      const float bb = (acc / 1.96875f) * height_scale;
+      b[(size_t)y * W + x] = bb;
+      if (d) d[(size_t)y * W + x] = glsl_max0(fill - bb);
+    }
+}
+
+// Rain-disk centres: disk k draws two outputs of the PCG32 stream
+// (seed, 1000 + k): cx = r + u0 % (W - 2r), cy = r + u1 % (H - 2r), so the
+// disk lies inside the grid (centre of the grid if it does not fit).
+void tws_oracle_rain_centers(uint64_t seed, int W, int H, int radius, int count, int* cx,
+                             int* cy) {
+  for (int k = 0; k < count; ++k) {
+    Pcg32 g;
+    g.seed(seed, 1000u + (uint64_t)k);
+    const uint32_t u0 = g.next(), u1 = g.next();
+    cx[k] = (W > 2 * radius) ? radius + (int)(u0 % (uint32_t)(W - 2 * radius)) : W / 2;
+    cy[k] = (H > 2 * radius) ? radius + (int)(u1 % (uint32_t)(H - 2 * radius)) : H / 2;
+  }
+}
+
+// Raw PCG32 outputs (for the known-answer test of the generator itself).
+void tws_oracle_pcg32(uint64_t initstate, uint64_t initseq, uint64_t skip, int n, uint32_t* out) {
+  Pcg32 g;
+  g.seed(initstate, initseq);
+  g.advance(skip);
+  for (int k = 0; k < n; ++k) out[k] = g.next();
+}
+
+// Parameter derivations.
+// Benchmark form: Kf = damping per step, Ka = dt*g*A/l, C = dt/l^2, evaluated in
+// double (simulationCommon.glsl:8-11 states these formulas).
+void tws_oracle_params_physical(double dt, double g, double A, double l, double damping,
+                                double out[3]) {
+  out[0] = damping;
+  out[1] = dt * g * A / l;
+  out[2] = dt / (l * l);
+}
+// Reference form, Terrain.cpp:175-198: step = 1/steps_per_second (float, held
+// as double seconds), cellDistance = world/res (float);
+// Kf = powf(damping, (float)step), Ka = (float)(step*accel*cellDistance),
+// C = (float)(step / (cellDistance*cellDistance)).
+void tws_oracle_params_reference(float steps_per_second, float damping, float accel,
+                                 float world_size, unsigned resolution, float out[3]) {
+  const double step = (double)(1.0f / steps_per_second);
+  const float cell = world_size / (float)resolution;
+  out[0] = powf(damping, (float)step);
+  out[1] = (float)(step * (double)accel * (double)cell);
+  out[2] = (float)(step / (double)(cell * cell));
+}
+
+// One or more steps in FP32, in place on b/d/f/v (row-major W x H; f holds 4
+// floats per cell, v 2 floats per cell, v may be NULL).  Returns elapsed
+// seconds of the step loop (steady clock).
+// flux_scale > 0 selects FP16 flux storage with that power-of-two scale
+// (the caller stores the initial flux already quantized).
+double tws_oracle_step_f32(int W, int H, float kf, float ka, float c, int closed, float flux_scale,
+                           const float* b, float* d, float* f, float* v,
+                           const tws_oracle_source* src, int nsrc, int nsteps, int nthreads) {
+  Params<float> p{kf, ka, c, closed, flux_scale};
+  const int nth = num_threads(nthreads);
+  const auto t0 = std::chrono::steady_clock::now();
+  run_steps<float>(W, H, p, b, d, reinterpret_cast<F4<float>*>(f), reinterpret_cast<F2<float>*>(v),
+                   src, nsrc, nsteps, nth);
+  const auto t1 = std::chrono::steady_clock::now();
+  return std::chrono::duration<double>(t1 - t0).count();
+}
+
+double tws_oracle_step_f64(int W, int H, double kf, double ka, double c, int closed,
+                           const double* b, double* d, double* f, double* v,
+                           const tws_oracle_source* src, int nsrc, int nsteps, int nthreads) {
+  Params<double> p{kf, ka, c, closed, 0.0};
+  const int nth = num_threads(nthreads);
+  const auto t0 = std::chrono::steady_clock::now();
+  run_steps<double>(W, H, p, b, d, reinterpret_cast<F4<double>*>(f),
+                    reinterpret_cast<F2<double>*>(v), src, nsrc, nsteps, nth);
+  const auto t1 = std::chrono::steady_clock::now();
+  return std::chrono::duration<double>(t1 - t0).count();
+}
+
+// Quantize a flux array to FP16 storage values in place (n floats).
+void tws_oracle_quantize_f16(float* f, long long n, float scale) {
+  for (long long i = 0; i < n; ++i) f[i] = quantize_half(f[i], scale);
+}
+
+// Only the source term (the reference's one-shot brush dispatch, Terrain.cpp:150-168).
+void tws_oracle_sources_f32(int W, int H, float* d, const tws_oracle_source* src, int nsrc) {
+  apply_sources<float>(W, H, d, src, nsrc, num_threads(0));
+}
+
+// Total water volume, sum of d in FP64 in row-major order, times the cell area.
+double tws_oracle_volume_f32(const float* d, long long n, double cell_area) {
+  double s = 0.0;
+  for (long long i = 0; i < n; ++i) s += (double)d[i];
+  return s * cell_area;
+}
+double tws_oracle_volume_f64(const double* d, long long n, double cell_area) {
+  double s = 0.0;
+  for (long long i = 0; i < n; ++i) s += d[i];
+  return s * cell_area;
+}
+
+int tws_oracle_max_threads(void) { return num_threads(0); }
+
+}  // extern "C"

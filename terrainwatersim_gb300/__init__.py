@@ -1,0 +1,277 @@
+"""terrainwatersim_gb300 -- GB300-native virtual-pipe shallow-water step.
+
+Python binding (ctypes) of the C ABI in include/tws.h.  The computation runs
+in libtws.so (hand-written sm_103a kernels); this module only marshals
+arguments.  There is no CPU fallback: if libtws.so has not been built, or no
+sm_103a GPU is present, the calls raise.
+
+The names follow the reference's `Terrain` class
+(terrainwatersim/source/scene/Terrain.h:15-153): a `Grid` is created from a
+heightmap, advanced with `step`, given water with `apply_source` (the
+reference's brush) or per-step `set_sources` (the benchmark's rain), and
+exposes its depth / flux / flow-map buffers.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+__all__ = [
+    "TwsError", "SimParams", "Source", "Buffers", "Grid", "lib", "library_path",
+    "params_physical", "params_reference", "rain_disks",
+    "BOUNDARY_CLOSED", "BOUNDARY_OPEN", "FLUX_F32", "FLUX_F16", "SOURCE_DISK", "SOURCE_BRUSH",
+    "MAX_SOURCES",
+]
+
+BOUNDARY_CLOSED = 0
+BOUNDARY_OPEN = 1
+FLUX_F32 = 0
+FLUX_F16 = 1
+SOURCE_DISK = 0
+SOURCE_BRUSH = 1
+MAX_SOURCES = 8
+
+TWS_OK = 0
+ERR_INVALID = -1
+ERR_CUDA = -2
+ERR_OOM = -3
+ERR_TIMEOUT = -4
+ERR_UNSUPPORTED = -5
+ERR_BUSY = -6
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_PKG, "_build", "libtws.so")
+_lock = threading.Lock()
+_lib = None
+
+
+class TwsError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"tws error {code}: {message}")
+        self.code = code
+
+
+class SimParams(C.Structure):
+    _fields_ = [("flow_friction_per_step", C.c_float),
+                ("water_acceleration_per_step", C.c_float),
+                ("cell_area_inv_time_scaled", C.c_float),
+                ("cell_area", C.c_float),
+                ("boundary", C.c_int)]
+
+    def as_tuple(self):
+        return (self.flow_friction_per_step, self.water_acceleration_per_step,
+                self.cell_area_inv_time_scaled)
+
+
+class Source(C.Structure):
+    _fields_ = [("kind", C.c_int), ("cx", C.c_float), ("cy", C.c_float),
+                ("radius", C.c_float), ("rate", C.c_float)]
+
+
+class Buffers(C.Structure):
+    _fields_ = [("terrain", C.c_void_p), ("depth", C.c_void_p), ("flux", C.c_void_p),
+                ("velocity", C.c_void_p), ("width", C.c_int), ("height", C.c_int),
+                ("pitch", C.c_int), ("flux_storage", C.c_int), ("flux_scale", C.c_float)]
+
+
+def library_path() -> str:
+    return _LIB_PATH
+
+
+def _declare(L):
+    vp, i, f, d, u64 = C.c_void_p, C.c_int, C.c_float, C.c_double, C.c_uint64
+    sig = {
+        "tws_params_physical": ([d, d, d, d, d, i, vp], i),
+        "tws_params_reference": ([f, f, f, f, C.c_uint, i, vp], i),
+        "tws_create": ([i, i, vp, i, vp, vp], i),
+        "tws_destroy": ([vp], i),
+        "tws_upload": ([vp, vp, vp, vp], i),
+        "tws_upload_device": ([vp, vp, vp, vp], i),
+        "tws_generate_scene": ([vp, u64, f, f], i),
+        "tws_scene_rain_disks": ([u64, i, i, i, f, i, vp], i),
+        "tws_set_params": ([vp, vp], i),
+        "tws_set_sources": ([vp, vp, i], i),
+        "tws_apply_source": ([vp, vp], i),
+        "tws_set_steps_per_launch": ([vp, i], i),
+        "tws_step": ([vp, i], i),
+        "tws_volume": ([vp, vp], i),
+        "tws_download": ([vp, vp, vp, vp], i),
+        "tws_download_terrain": ([vp, vp], i),
+        "tws_get_buffers": ([vp, vp], i),
+        "tws_sync": ([vp], i),
+        "tws_stream": ([vp], vp),
+        "tws_error_string": ([i], C.c_char_p),
+        "tws_last_error": ([vp], C.c_char_p),
+        "tws_launch_count": ([], u64),
+        "tws_version": ([], C.c_char_p),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+
+
+def lib():
+    """Load libtws.so (built by terrainwatersim_gb300.build).  Raises if absent."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(_LIB_PATH):
+                raise RuntimeError(
+                    f"{_LIB_PATH} is missing: build it with "
+                    "`python -c 'import __graft_entry__ as g; g.build()'` (there is no CPU fallback)")
+            L = C.CDLL(_LIB_PATH)
+            _declare(L)
+            _lib = L
+    return _lib
+
+
+def _check(code: int, grid_handle=None):
+    if code != TWS_OK:
+        L = lib()
+        msg = L.tws_last_error(grid_handle).decode() if grid_handle else ""
+        raise TwsError(code, f"{L.tws_error_string(code).decode()}: {msg}")
+
+
+def params_physical(dt=0.02, gravity=9.81, pipe_area=1.0, cell_size=1.0, damping_per_step=0.998,
+                    boundary=BOUNDARY_CLOSED) -> SimParams:
+    p = SimParams()
+    _check(lib().tws_params_physical(dt, gravity, pipe_area, cell_size, damping_per_step, boundary,
+                                     C.byref(p)))
+    return p
+
+
+def params_reference(steps_per_second=60.0, flow_damping=0.98, flow_acceleration=10.0,
+                     grid_world_size=1024.0, grid_resolution=1024,
+                     boundary=BOUNDARY_OPEN) -> SimParams:
+    p = SimParams()
+    _check(lib().tws_params_reference(steps_per_second, flow_damping, flow_acceleration,
+                                      grid_world_size, grid_resolution, boundary, C.byref(p)))
+    return p
+
+
+def rain_disks(seed: int, width: int, height: int, radius: int, rate: float, count: int = 1):
+    arr = (Source * max(1, count))()
+    _check(lib().tws_scene_rain_disks(seed, width, height, radius, rate, count, arr))
+    return [(s.kind, s.cx, s.cy, s.radius, s.rate) for s in arr[:count]]
+
+
+def _host_f32(a, shape):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if a.shape != shape:
+        raise ValueError(f"expected shape {shape}, got {a.shape}")
+    return a
+
+
+class Grid:
+    """One simulated grid resident on the GPU (the simulation half of Terrain)."""
+
+    def __init__(self, width: int, height: int, params: SimParams | None = None,
+                 flux_storage: int = FLUX_F32, stream: int | None = None):
+        self.width, self.height = int(width), int(height)
+        self.params = params if params is not None else params_physical()
+        self.flux_storage = flux_storage
+        h = C.c_void_p()
+        _check(lib().tws_create(self.width, self.height, C.byref(self.params), flux_storage,
+                                C.c_void_p(stream) if stream else None, C.byref(h)))
+        self._h = h
+
+    # -- lifecycle
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().tws_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def stream(self) -> int:
+        return lib().tws_stream(self._h) or 0
+
+    # -- state
+    def upload(self, terrain, depth=None, flux=None):
+        H, W = self.height, self.width
+        b = _host_f32(terrain, (H, W))
+        d = _host_f32(depth, (H, W)) if depth is not None else None
+        f = _host_f32(flux, (H, W, 4)) if flux is not None else None
+        _check(lib().tws_upload(self._h, b.ctypes.data,
+                                d.ctypes.data if d is not None else None,
+                                f.ctypes.data if f is not None else None), self._h)
+
+    def upload_device(self, terrain_ptr: int, depth_ptr: int | None = None,
+                      flux_ptr: int | None = None):
+        _check(lib().tws_upload_device(self._h, terrain_ptr, depth_ptr, flux_ptr), self._h)
+
+    def generate_scene(self, seed: int, height_scale: float = 40.0, fill: float = 15.0):
+        _check(lib().tws_generate_scene(self._h, seed, height_scale, fill), self._h)
+
+    def set_params(self, params: SimParams):
+        _check(lib().tws_set_params(self._h, C.byref(params)), self._h)
+        self.params = params
+
+    def set_sources(self, sources):
+        srcs = list(sources)
+        arr = (Source * max(1, len(srcs)))()
+        for k, s in enumerate(srcs):
+            arr[k] = Source(*s)
+        _check(lib().tws_set_sources(self._h, arr, len(srcs)), self._h)
+
+    def apply_source(self, source):
+        s = Source(*source)
+        _check(lib().tws_apply_source(self._h, C.byref(s)), self._h)
+
+    def set_steps_per_launch(self, k: int):
+        _check(lib().tws_set_steps_per_launch(self._h, k), self._h)
+
+    def step(self, nsteps: int = 1):
+        _check(lib().tws_step(self._h, nsteps), self._h)
+
+    def volume(self) -> float:
+        out = C.c_double()
+        _check(lib().tws_volume(self._h, C.byref(out)), self._h)
+        return out.value
+
+    def sync(self):
+        _check(lib().tws_sync(self._h), self._h)
+
+    def download(self, depth=True, flux=True, velocity=True, out=None):
+        """Return (d, f, v) as float32 host arrays (None where not requested).
+        `out` may supply preallocated (d, f, v) arrays."""
+        H, W = self.height, self.width
+        if out is not None:
+            d, f, v = out
+        else:
+            d = np.empty((H, W), np.float32) if depth else None
+            f = np.empty((H, W, 4), np.float32) if flux else None
+            v = np.empty((H, W, 2), np.float32) if velocity else None
+        _check(lib().tws_download(self._h, d.ctypes.data if d is not None else None,
+                                  f.ctypes.data if f is not None else None,
+                                  v.ctypes.data if v is not None else None), self._h)
+        return d, f, v
+
+    def download_terrain(self):
+        b = np.empty((self.height, self.width), np.float32)
+        _check(lib().tws_download_terrain(self._h, b.ctypes.data), self._h)
+        return b
+
+    def buffers(self) -> Buffers:
+        out = Buffers()
+        _check(lib().tws_get_buffers(self._h, C.byref(out)), self._h)
+        return out

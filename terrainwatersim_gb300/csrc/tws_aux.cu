@@ -1,0 +1,322 @@
+// tws_aux.cu -- the kernels around the step: one-shot sources, the FP64 total
+// volume, the synthetic scene generator and flux format conversion.
+
+#include <algorithm>
+
+#include "tws_device.cuh"
+#include "tws_internal.h"
+
+namespace tws {
+namespace {
+
+// ---- one-shot source (the reference's brush dispatch, Terrain.cpp:150-168) --
+__global__ void apply_source_kernel(float* d, int W, int H, int pitch, StepArgs a) {
+  const int gx = a.src[0].bx0 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int gy = a.src[0].by0 + blockIdx.y * blockDim.y + threadIdx.y;
+  if (gx > a.src[0].bx1 || gy > a.src[0].by1 || gx >= W || gy >= H) return;
+  const size_t g = (size_t)gy * pitch + gx;
+  d[g] = add_sources(d[g], gx, gy, a, 1u);
+}
+
+// ---- total volume in FP64 ---------------------------------------------------
+// Two passes with a fixed partition and a fixed reduction tree, so the result
+// is deterministic for a given grid size.  Pass 1: block r sums rows
+// r, r + gridDim.x, ... into partials[r].  Pass 2: one block sums partials.
+constexpr int kVolThreads = 256;
+constexpr int kVolMaxBlocks = 1024;
+
+__device__ double block_sum(double v) {
+  __shared__ double warp_part[kVolThreads / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) warp_part[wid] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (wid == 0) {
+    s = lane < kVolThreads / 32 ? warp_part[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  }
+  return s;  // valid in thread 0
+}
+
+__global__ void __launch_bounds__(kVolThreads)
+    volume_rows_kernel(const float* d, int W, int H, int pitch, double* partials) {
+  double acc = 0.0;
+  for (int y = blockIdx.x; y < H; y += gridDim.x) {
+    const float* row = d + (size_t)y * pitch;
+    for (int x = threadIdx.x; x < W; x += kVolThreads) acc += (double)row[x];
+  }
+  const double s = block_sum(acc);
+  if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(kVolThreads)
+    volume_final_kernel(const double* partials, int n, double cell_area, double* out) {
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < n; i += kVolThreads) acc += partials[i];
+  const double s = block_sum(acc);
+  if (threadIdx.x == 0) *out = s * cell_area;
+}
+
+// ---- scene generator ----------------------------------------------------------
+// Seeded PCG32 value noise, the definition the oracle's generator states:
+// octave o (0..5) has lattice spacing 64 >> o; its lattice value (i, j) is
+// output number j*Lx + i of the PCG32 stream (seed, o + 1), Lx = W/s + 2,
+// mapped to [0, 1) with 24 bits; smoothstep-bilinear interpolation; octave
+// amplitudes 1, 1/2, ...; sum / 1.96875 * height_scale.
+// PCG32 is O'Neill's XSH-RR 64/32 generator; lattice points are generated in
+// parallel by jumping the LCG ahead (Brown 1994).
+constexpr int kOctaves = 6;
+}  // namespace
+
+constexpr uint64_t kPcgMult = 6364136223846793005ULL;
+
+struct Pcg32 {
+  uint64_t state, inc;
+  __host__ __device__ void seed(uint64_t initstate, uint64_t initseq) {
+    state = 0u;
+    inc = (initseq << 1u) | 1u;
+    next();
+    state += initstate;
+    next();
+  }
+  __host__ __device__ uint32_t next() {
+    const uint64_t old = state;
+    state = old * kPcgMult + inc;
+    const uint32_t xorshifted = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+    const uint32_t rot = (uint32_t)(old >> 59u);
+    return (xorshifted >> rot) | (xorshifted << ((0u - rot) & 31u));
+  }
+  __host__ __device__ void advance(uint64_t delta) {
+    uint64_t cur_mult = kPcgMult, cur_plus = inc, acc_mult = 1u, acc_plus = 0u;
+    while (delta > 0) {
+      if (delta & 1u) {
+        acc_mult *= cur_mult;
+        acc_plus = acc_plus * cur_mult + cur_plus;
+      }
+      cur_plus = (cur_mult + 1u) * cur_plus;
+      cur_mult *= cur_mult;
+      delta >>= 1u;
+    }
+    state = acc_mult * state + acc_plus;
+  }
+};
+
+namespace {
+
+struct Lattice {
+  float* v[kOctaves];
+  int lx[kOctaves];
+  long long n[kOctaves];
+  uint64_t base_state[kOctaves], inc[kOctaves];
+};
+
+__global__ void lattice_kernel(Lattice L, int o) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= L.n[o]) return;
+  Pcg32 g;
+  g.state = L.base_state[o];
+  g.inc = L.inc[o];
+  g.advance((uint64_t)k);
+  L.v[o][k] = (float)(g.next() >> 8) * (1.0f / 16777216.0f);
+}
+
+__device__ __forceinline__ float smooth01(float t) {
+  return fmul(fmul(t, t), fsub(3.0f, fmul(2.0f, t)));
+}
+__device__ __forceinline__ float lerpf(float a, float b, float t) {
+  return fadd(a, fmul(fsub(b, a), t));
+}
+
+__global__ void scene_kernel(Lattice L, int W, int H, int pitch, float height_scale, float fill,
+                             float* b, float* d) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= W || y >= H) return;
+  float acc = 0.0f, amp = 1.0f;
+#pragma unroll
+  for (int o = 0; o < kOctaves; ++o) {
+    const int s = 64 >> o;
+    const float inv = 1.0f / (float)s;
+    const int i = x / s, j = y / s;
+    const float sx = smooth01(fmul((float)(x % s), inv));
+    const float sy = smooth01(fmul((float)(y % s), inv));
+    const float* V = L.v[o];
+    const int Lx = L.lx[o];
+    const float v00 = V[(size_t)j * Lx + i], v10 = V[(size_t)j * Lx + i + 1];
+    const float v01 = V[(size_t)(j + 1) * Lx + i], v11 = V[(size_t)(j + 1) * Lx + i + 1];
+    const float v = lerpf(lerpf(v00, v10, sx), lerpf(v01, v11, sx), sy);
+    acc = fadd(acc, fmul(amp, v));
+    amp = fmul(amp, 0.5f);
+  }
+  const float bb = fmul(fdiv(acc, 1.96875f), height_scale);
+  const size_t g = (size_t)y * pitch + x;
+  b[g] = bb;
+  d[g] = max0(fsub(fill, bb));
+}
+
+// ---- flux format conversion -----------------------------------------------------
+__global__ void flux_to_f32_kernel(const void* f, int f16, float inv_scale, int W, int H,
+                                   int pitch, float4* out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= W || y >= H) return;
+  const size_t g = (size_t)y * pitch + x;
+  float4 r;
+  if (f16) {
+    const __half2* h = reinterpret_cast<const __half2*>(f) + 2 * g;
+    const float2 lo = __half22float2(h[0]), hi = __half22float2(h[1]);
+    r = make_float4(fmul(lo.x, inv_scale), fmul(lo.y, inv_scale), fmul(hi.x, inv_scale),
+                    fmul(hi.y, inv_scale));
+  } else {
+    r = reinterpret_cast<const float4*>(f)[g];
+  }
+  out[(size_t)y * W + x] = r;
+}
+
+__global__ void flux_from_f32_kernel(const float4* in, int f16, float scale, int W, int H,
+                                     int pitch, void* f) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= W || y >= H) return;
+  const size_t g = (size_t)y * pitch + x;
+  const float4 v = in[(size_t)y * W + x];
+  if (f16) {
+    __half2* h = reinterpret_cast<__half2*>(f) + 2 * g;
+    h[0] = __floats2half2_rn(fminf(fmul(v.x, scale), 65504.0f), fminf(fmul(v.y, scale), 65504.0f));
+    h[1] = __floats2half2_rn(fminf(fmul(v.z, scale), 65504.0f), fminf(fmul(v.w, scale), 65504.0f));
+  } else {
+    reinterpret_cast<float4*>(f)[g] = v;
+  }
+}
+
+}  // namespace
+
+DevSource make_dev_source(const tws_source& s) {
+  DevSource r{};
+  r.kind = s.kind;
+  r.cx = s.cx;
+  r.cy = s.cy;
+  r.radius = s.radius;
+  r.rate = s.rate;
+  if (s.kind == TWS_SOURCE_DISK) {
+    r.icx = (int)s.cx;
+    r.icy = (int)s.cy;
+    r.ir = (int)s.radius;
+    r.bx0 = r.icx - r.ir;
+    r.bx1 = r.icx + r.ir;
+    r.by0 = r.icy - r.ir;
+    r.by1 = r.icy + r.ir;
+  } else {
+    // Every cell the brush can change satisfies |(x,y) - c|^2 < S (1 + eps);
+    // the box is widened by two cells beyond sqrt(S).
+    const float rr = sqrtf(s.radius > 0.0f ? s.radius : 0.0f);
+    r.bx0 = (int)floorf(s.cx - rr) - 2;
+    r.bx1 = (int)ceilf(s.cx + rr) + 2;
+    r.by0 = (int)floorf(s.cy - rr) - 2;
+    r.by1 = (int)ceilf(s.cy + rr) + 2;
+  }
+  return r;
+}
+
+cudaError_t launch_apply_source(float* d, int W, int H, int pitch, const DevSource& s,
+                                cudaStream_t st) {
+  StepArgs a{};
+  a.nsrc = 1;
+  a.src[0] = s;
+  a.src[0].bx0 = std::max(0, s.bx0);
+  a.src[0].by0 = std::max(0, s.by0);
+  a.src[0].bx1 = std::min(W - 1, s.bx1);
+  a.src[0].by1 = std::min(H - 1, s.by1);
+  if (a.src[0].bx0 > a.src[0].bx1 || a.src[0].by0 > a.src[0].by1) return cudaSuccess;
+  const int w = a.src[0].bx1 - a.src[0].bx0 + 1, h = a.src[0].by1 - a.src[0].by0 + 1;
+  dim3 blk(32, 8), grd((w + 31) / 32, (h + 7) / 8);
+  apply_source_kernel<<<grd, blk, 0, st>>>(d, W, H, pitch, a);
+  count_launch();
+  return cudaGetLastError();
+}
+
+int volume_partials_needed() { return kVolMaxBlocks; }
+
+cudaError_t launch_volume(const float* d, int W, int H, int pitch, double cell_area,
+                          double* partials, int max_partials, double* out, cudaStream_t st) {
+  const int nb = std::max(1, std::min({H, kVolMaxBlocks, max_partials}));
+  volume_rows_kernel<<<nb, kVolThreads, 0, st>>>(d, W, H, pitch, partials);
+  volume_final_kernel<<<1, kVolThreads, 0, st>>>(partials, nb, cell_area, out);
+  count_launch(2);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_generate_scene(uint64_t seed, int W, int H, int pitch, float height_scale,
+                                  float fill, float* b, float* d, cudaStream_t st) {
+  Lattice L{};
+  long long total = 0;
+  for (int o = 0; o < kOctaves; ++o) {
+    const int s = 64 >> o;
+    L.lx[o] = W / s + 2;
+    L.n[o] = (long long)L.lx[o] * (H / s + 2);
+    total += L.n[o];
+    Pcg32 g;
+    g.seed(seed, (uint64_t)o + 1u);
+    L.base_state[o] = g.state;
+    L.inc[o] = g.inc;
+  }
+  float* buf = nullptr;
+  cudaError_t e = cudaMallocAsync(&buf, (size_t)total * sizeof(float), st);
+  if (e != cudaSuccess) return e;
+  long long off = 0;
+  for (int o = 0; o < kOctaves; ++o) {
+    L.v[o] = buf + off;
+    off += L.n[o];
+  }
+  for (int o = 0; o < kOctaves; ++o) {
+    const int nb = (int)((L.n[o] + 255) / 256);
+    lattice_kernel<<<nb, 256, 0, st>>>(L, o);
+  }
+  dim3 blk(32, 8), grd((W + 31) / 32, (H + 7) / 8);
+  scene_kernel<<<grd, blk, 0, st>>>(L, W, H, pitch, height_scale, fill, b, d);
+  count_launch(kOctaves + 1);
+  e = cudaGetLastError();
+  cudaFreeAsync(buf, st);
+  return e;
+}
+
+cudaError_t launch_flux_to_f32(const void* f, int flux_storage, float inv_scale, int W, int H,
+                               int pitch, float* out_packed, cudaStream_t st) {
+  dim3 blk(32, 8), grd((W + 31) / 32, (H + 7) / 8);
+  flux_to_f32_kernel<<<grd, blk, 0, st>>>(f, flux_storage == TWS_FLUX_F16, inv_scale, W, H, pitch,
+                                          reinterpret_cast<float4*>(out_packed));
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_flux_from_f32(const float* in_packed, int flux_storage, float scale, int W,
+                                 int H, int pitch, void* f, cudaStream_t st) {
+  dim3 blk(32, 8), grd((W + 31) / 32, (H + 7) / 8);
+  flux_from_f32_kernel<<<grd, blk, 0, st>>>(reinterpret_cast<const float4*>(in_packed),
+                                            flux_storage == TWS_FLUX_F16, scale, W, H, pitch, f);
+  count_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace tws
+
+extern "C" TWS_API int tws_scene_rain_disks(uint64_t seed, int W, int H, int radius, float rate,
+                                            int count, tws_source* out) {
+  if (!out || W < 1 || H < 1 || radius < 0 || count < 0 || !(rate == rate)) return TWS_ERR_INVALID;
+  for (int k = 0; k < count; ++k) {
+    tws::Pcg32 g;
+    g.seed(seed, 1000u + (uint64_t)k);
+    const uint32_t u0 = g.next(), u1 = g.next();
+    const int cx = (W > 2 * radius) ? radius + (int)(u0 % (uint32_t)(W - 2 * radius)) : W / 2;
+    const int cy = (H > 2 * radius) ? radius + (int)(u1 % (uint32_t)(H - 2 * radius)) : H / 2;
+    out[k].kind = TWS_SOURCE_DISK;
+    out[k].cx = (float)cx;
+    out[k].cy = (float)cy;
+    out[k].radius = (float)radius;
+    out[k].rate = rate;
+  }
+  return TWS_OK;
+}

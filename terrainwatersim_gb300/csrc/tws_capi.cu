@@ -1,0 +1,469 @@
+// tws_capi.cu -- the C ABI (include/tws.h): grid lifecycle, uploads,
+// parameter derivation and step scheduling.  Host code only; kernels live in
+// tws_step.cu and tws_aux.cu.
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "tws_internal.h"
+
+namespace tws {
+
+static std::atomic<uint64_t> g_launches{0};
+void count_launch(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+}  // namespace tws
+
+using namespace tws;
+
+// Maps for one kernel variant; encoded on first use and cached.
+struct VariantMaps {
+  bool ready = false;
+  CUtensorMap b, d[2], f[2];
+};
+
+struct tws_grid {
+  int W = 0, H = 0, pitch = 0;
+  tws_sim_params params{};
+  int flux_storage = TWS_FLUX_F32;
+  float flux_scale = 1.0f;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int device = 0;
+  float* b = nullptr;
+  float* d[2] = {nullptr, nullptr};
+  void* f[2] = {nullptr, nullptr};
+  float2* v = nullptr;
+  int cur = 0;
+  int steps_per_launch = 0;  // 0: library's choice
+  std::vector<VariantMaps> maps;
+  tws_source src[TWS_MAX_SOURCES];
+  int nsrc = 0;
+  double* vol_partials = nullptr;
+  double* vol_out = nullptr;
+  double* vol_host = nullptr;  // pinned
+  int* err = nullptr;          // device error word
+  int* err_host = nullptr;     // pinned
+  std::string last_error;
+};
+
+namespace {
+
+int fail(tws_grid* g, int code, const std::string& msg) {
+  if (g) g->last_error = msg;
+  return code;
+}
+
+int cuda_fail(tws_grid* g, cudaError_t e, const char* what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  return fail(g, e == cudaErrorMemoryAllocation ? TWS_ERR_OOM : TWS_ERR_CUDA, m);
+}
+
+#define TWS_CUDA(g, call, what)                  \
+  do {                                           \
+    cudaError_t e_ = (call);                     \
+    if (e_ != cudaSuccess) return cuda_fail(g, e_, what); \
+  } while (0)
+
+size_t flux_bytes_per_cell(int storage) { return storage == TWS_FLUX_F16 ? 8 : 16; }
+
+bool params_ok(const tws_sim_params* p) {
+  if (!p) return false;
+  if (p->boundary != TWS_BOUNDARY_CLOSED && p->boundary != TWS_BOUNDARY_OPEN) return false;
+  return std::isfinite(p->flow_friction_per_step) && std::isfinite(p->water_acceleration_per_step) &&
+         std::isfinite(p->cell_area_inv_time_scaled) && std::isfinite(p->cell_area);
+}
+
+// Default F16 scale: a power of two that puts the largest possible outflow
+// (d_max / C, reached when the scaling of flowUpdate.comp:57-59 engages) at
+// about 2^13, leaving headroom for depth growth from sources.
+float pick_flux_scale(float d_max, float c) {
+  const double fmax = std::max(1.0, (double)d_max) / std::max(1e-12, (double)c);
+  const int e = (int)std::floor(std::log2(8192.0 / fmax));
+  return std::ldexp(1.0f, std::max(-24, std::min(24, e)));
+}
+
+VariantMaps* maps_for(tws_grid* g, int variant, std::string* why) {
+  if ((int)g->maps.size() < step_variant_count()) g->maps.resize(step_variant_count());
+  VariantMaps& m = g->maps[variant];
+  if (!m.ready) {
+    for (int i = 0; i < 2; ++i) {
+      cudaError_t e = encode_step_maps(variant, g->flux_storage, g->W, g->H, g->pitch,
+                                       i == 0 ? g->b : nullptr, g->d[i], g->f[i], &m.b, &m.d[i],
+                                       &m.f[i], why);
+      if (e != cudaSuccess) return nullptr;
+    }
+    m.ready = true;
+  }
+  return &m;
+}
+
+int default_steps_per_launch(const tws_grid* g) {
+  // Temporal blocking pays once the grid no longer fits in L2 (129 MB);
+  // small grids are launch-bound and take the plain kernel.
+  const double bytes = (double)g->W * g->H * (16.0 + flux_bytes_per_cell(g->flux_storage) * 2 + 8);
+  return bytes > 64e6 ? 2 : 1;
+}
+
+int enqueue_steps(tws_grid* g, int nsteps) {
+  StepArgs a{};
+  a.W = g->W;
+  a.H = g->H;
+  a.pitch = g->pitch;
+  a.kf = g->params.flow_friction_per_step;
+  a.ka = g->params.water_acceleration_per_step;
+  a.c = g->params.cell_area_inv_time_scaled;
+  a.closed = g->params.boundary == TWS_BOUNDARY_CLOSED;
+  a.nsrc = g->nsrc;
+  for (int i = 0; i < g->nsrc; ++i) a.src[i] = make_dev_source(g->src[i]);
+  a.v_out = g->v;
+  a.flux_scale = g->flux_scale;
+  a.flux_inv_scale = 1.0f / g->flux_scale;
+  a.err = g->err;
+  const int kmax = g->steps_per_launch > 0 ? g->steps_per_launch : default_steps_per_launch(g);
+  int left = nsteps;
+  std::string why;
+  while (left > 0) {
+    const int k = std::min(kmax, left);
+    const int variant = step_variant_for(k, g->flux_storage);
+    VariantMaps* m = maps_for(g, variant, &why);
+    if (!m) return fail(g, TWS_ERR_CUDA, why);
+    const int nxt = g->cur ^ 1;
+    a.d_out = g->d[nxt];
+    a.f_out = g->f[nxt];
+    cudaError_t e = launch_step(variant, g->flux_storage, m->b, m->d[g->cur], m->f[g->cur], a,
+                                g->stream);
+    if (e != cudaSuccess) return cuda_fail(g, e, "step kernel launch");
+    g->cur = nxt;
+    left -= k;
+  }
+  return TWS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+TWS_API const char* tws_version(void) { return "terrainwatersim-gb300 0.1 (sm_103a)"; }
+
+TWS_API uint64_t tws_launch_count(void) { return g_launches.load(); }
+
+TWS_API const char* tws_error_string(int code) {
+  switch (code) {
+    case TWS_OK: return "ok";
+    case TWS_ERR_INVALID: return "invalid argument";
+    case TWS_ERR_CUDA: return "CUDA error";
+    case TWS_ERR_OOM: return "out of device memory";
+    case TWS_ERR_TIMEOUT: return "device-side wait timed out";
+    case TWS_ERR_UNSUPPORTED: return "unsupported option";
+    case TWS_ERR_BUSY: return "admission refused";
+    default: return "unknown error";
+  }
+}
+
+TWS_API const char* tws_last_error(tws_grid* g) { return g ? g->last_error.c_str() : "null grid"; }
+
+TWS_API int tws_params_physical(double dt, double gravity, double pipe_area, double cell_size,
+                                double damping_per_step, int boundary, tws_sim_params* out) {
+  if (!out || !(dt > 0) || !(cell_size > 0) || !(pipe_area > 0) || !std::isfinite(gravity) ||
+      !std::isfinite(damping_per_step))
+    return TWS_ERR_INVALID;
+  if (boundary != TWS_BOUNDARY_CLOSED && boundary != TWS_BOUNDARY_OPEN) return TWS_ERR_INVALID;
+  out->flow_friction_per_step = (float)damping_per_step;
+  out->water_acceleration_per_step = (float)(dt * gravity * pipe_area / cell_size);
+  out->cell_area_inv_time_scaled = (float)(dt / (cell_size * cell_size));
+  out->cell_area = (float)(cell_size * cell_size);
+  out->boundary = boundary;
+  return TWS_OK;
+}
+
+TWS_API int tws_params_reference(float steps_per_second, float flow_damping,
+                                 float flow_acceleration, float grid_world_size,
+                                 unsigned grid_resolution, int boundary, tws_sim_params* out) {
+  if (!out || !(steps_per_second > 0) || grid_resolution == 0 || !(grid_world_size > 0))
+    return TWS_ERR_INVALID;
+  if (boundary != TWS_BOUNDARY_CLOSED && boundary != TWS_BOUNDARY_OPEN) return TWS_ERR_INVALID;
+  // Terrain.cpp:177 -- the step length is a float 1/steps held as double seconds.
+  const double step = (double)(1.0f / steps_per_second);
+  // Terrain.cpp:183, 196
+  const float cell = grid_world_size / (float)grid_resolution;
+  out->flow_friction_per_step = powf(flow_damping, (float)step);                      // :190
+  out->water_acceleration_per_step = (float)(step * (double)flow_acceleration * (double)cell);  // :197
+  out->cell_area_inv_time_scaled = (float)(step / (double)(cell * cell));            // :184
+  out->cell_area = cell * cell;
+  out->boundary = boundary;
+  return TWS_OK;
+}
+
+TWS_API int tws_create(int width, int height, const tws_sim_params* params, int flux_storage,
+                       void* stream, tws_grid** out) {
+  if (!out) return TWS_ERR_INVALID;
+  *out = nullptr;
+  if (width < 1 || height < 1 || width > (1 << 20) || height > (1 << 20) || !params_ok(params))
+    return TWS_ERR_INVALID;
+  if (flux_storage != TWS_FLUX_F32 && flux_storage != TWS_FLUX_F16) return TWS_ERR_INVALID;
+  tws_grid* g = new (std::nothrow) tws_grid();
+  if (!g) return TWS_ERR_OOM;
+  g->W = width;
+  g->H = height;
+  g->pitch = (width + 31) / 32 * 32;
+  g->params = *params;
+  g->flux_storage = flux_storage;
+  g->flux_scale = flux_storage == TWS_FLUX_F16
+                      ? pick_flux_scale(32.0f, params->cell_area_inv_time_scaled)
+                      : 1.0f;
+  auto bail = [&](int code) {
+    tws_destroy(g);
+    return code;
+  };
+  cudaError_t e = cudaGetDevice(&g->device);
+  if (e != cudaSuccess) return bail(TWS_ERR_CUDA);
+  int major = 0, minor = 0;
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, g->device);
+  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, g->device);
+  if (major != 10 || minor != 3) {
+    // The kernels are built for sm_103a only.
+    return bail(TWS_ERR_CUDA);
+  }
+  if (stream) {
+    g->stream = static_cast<cudaStream_t>(stream);
+  } else {
+    if (cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) != cudaSuccess)
+      return bail(TWS_ERR_CUDA);
+    g->own_stream = true;
+  }
+  const size_t n = (size_t)g->pitch * g->H;
+  const size_t fb = flux_bytes_per_cell(flux_storage);
+  if (cudaMalloc(&g->b, n * 4) != cudaSuccess || cudaMalloc(&g->d[0], n * 4) != cudaSuccess ||
+      cudaMalloc(&g->d[1], n * 4) != cudaSuccess || cudaMalloc(&g->f[0], n * fb) != cudaSuccess ||
+      cudaMalloc(&g->f[1], n * fb) != cudaSuccess || cudaMalloc(&g->v, n * 8) != cudaSuccess ||
+      cudaMalloc(&g->vol_partials, sizeof(double) * volume_partials_needed()) != cudaSuccess ||
+      cudaMalloc(&g->vol_out, sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&g->err, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    return bail(TWS_ERR_OOM);
+  }
+  if (cudaMallocHost(&g->vol_host, sizeof(double)) != cudaSuccess ||
+      cudaMallocHost(&g->err_host, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    return bail(TWS_ERR_OOM);
+  }
+  // Zero everything, padding included (the F16 flux map reads the padding
+  // cell of odd-width rows and relies on it staying zero).
+  cudaMemsetAsync(g->b, 0, n * 4, g->stream);
+  cudaMemsetAsync(g->d[0], 0, n * 4, g->stream);
+  cudaMemsetAsync(g->d[1], 0, n * 4, g->stream);
+  cudaMemsetAsync(g->f[0], 0, n * fb, g->stream);
+  cudaMemsetAsync(g->f[1], 0, n * fb, g->stream);
+  cudaMemsetAsync(g->v, 0, n * 8, g->stream);
+  cudaMemsetAsync(g->err, 0, sizeof(int), g->stream);
+  if (cudaStreamSynchronize(g->stream) != cudaSuccess) return bail(TWS_ERR_CUDA);
+  *out = g;
+  return TWS_OK;
+}
+
+TWS_API int tws_destroy(tws_grid* g) {
+  if (!g) return TWS_ERR_INVALID;
+  if (g->stream) cudaStreamSynchronize(g->stream);
+  cudaFree(g->b);
+  cudaFree(g->d[0]);
+  cudaFree(g->d[1]);
+  cudaFree(g->f[0]);
+  cudaFree(g->f[1]);
+  cudaFree(g->v);
+  cudaFree(g->vol_partials);
+  cudaFree(g->vol_out);
+  cudaFree(g->err);
+  if (g->vol_host) cudaFreeHost(g->vol_host);
+  if (g->err_host) cudaFreeHost(g->err_host);
+  if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
+  delete g;
+  return TWS_OK;
+}
+
+TWS_API void* tws_stream(tws_grid* g) { return g ? (void*)g->stream : nullptr; }
+
+static int upload_impl(tws_grid* g, const float* b, const float* d, const float* f,
+                       cudaMemcpyKind kind) {
+  if (!g || !b) return fail(g, TWS_ERR_INVALID, "terrain array is required");
+  const size_t row = (size_t)g->W * 4, pitch = (size_t)g->pitch * 4;
+  const size_t n = (size_t)g->pitch * g->H;
+  g->cur = 0;
+  TWS_CUDA(g, cudaMemcpy2DAsync(g->b, pitch, b, row, row, g->H, kind, g->stream), "upload terrain");
+  if (d)
+    TWS_CUDA(g, cudaMemcpy2DAsync(g->d[0], pitch, d, row, row, g->H, kind, g->stream), "upload depth");
+  else
+    TWS_CUDA(g, cudaMemsetAsync(g->d[0], 0, n * 4, g->stream), "clear depth");
+  const size_t fb = flux_bytes_per_cell(g->flux_storage);
+  if (f) {
+    if (g->flux_storage == TWS_FLUX_F32) {
+      TWS_CUDA(g, cudaMemcpy2DAsync(g->f[0], (size_t)g->pitch * 16, f, (size_t)g->W * 16,
+                                    (size_t)g->W * 16, g->H, kind, g->stream),
+               "upload flux");
+    } else {
+      float* tmp = nullptr;
+      TWS_CUDA(g, cudaMallocAsync(&tmp, (size_t)g->W * g->H * 16, g->stream), "flux staging");
+      cudaMemcpyAsync(tmp, f, (size_t)g->W * g->H * 16, kind, g->stream);
+      launch_flux_from_f32(tmp, g->flux_storage, g->flux_scale, g->W, g->H, g->pitch, g->f[0],
+                           g->stream);
+      cudaFreeAsync(tmp, g->stream);
+    }
+  } else {
+    TWS_CUDA(g, cudaMemsetAsync(g->f[0], 0, n * fb, g->stream), "clear flux");
+  }
+  TWS_CUDA(g, cudaMemsetAsync(g->v, 0, n * 8, g->stream), "clear velocity");
+  TWS_CUDA(g, cudaStreamSynchronize(g->stream), "upload");
+  return TWS_OK;
+}
+
+TWS_API int tws_upload(tws_grid* g, const float* b, const float* d, const float* f) {
+  return upload_impl(g, b, d, f, cudaMemcpyHostToDevice);
+}
+
+TWS_API int tws_upload_device(tws_grid* g, const float* b, const float* d, const float* f) {
+  return upload_impl(g, b, d, f, cudaMemcpyDeviceToDevice);
+}
+
+TWS_API int tws_generate_scene(tws_grid* g, uint64_t seed, float height_scale, float fill) {
+  if (!g || !(height_scale >= 0) || !std::isfinite(fill)) return fail(g, TWS_ERR_INVALID, "bad scene");
+  const size_t n = (size_t)g->pitch * g->H;
+  g->cur = 0;
+  TWS_CUDA(g, launch_generate_scene(seed, g->W, g->H, g->pitch, height_scale, fill, g->b, g->d[0],
+                                    g->stream),
+           "scene generator");
+  TWS_CUDA(g, cudaMemsetAsync(g->f[0], 0, n * flux_bytes_per_cell(g->flux_storage), g->stream),
+           "clear flux");
+  TWS_CUDA(g, cudaMemsetAsync(g->v, 0, n * 8, g->stream), "clear velocity");
+  return TWS_OK;
+}
+
+TWS_API int tws_set_params(tws_grid* g, const tws_sim_params* p) {
+  if (!g || !params_ok(p)) return fail(g, TWS_ERR_INVALID, "bad parameters");
+  g->params = *p;
+  return TWS_OK;
+}
+
+TWS_API int tws_set_sources(tws_grid* g, const tws_source* s, int n) {
+  if (!g || n < 0 || n > TWS_MAX_SOURCES || (n > 0 && !s))
+    return fail(g, TWS_ERR_INVALID, "bad source list");
+  for (int i = 0; i < n; ++i) {
+    if (s[i].kind != TWS_SOURCE_DISK && s[i].kind != TWS_SOURCE_BRUSH)
+      return fail(g, TWS_ERR_INVALID, "bad source kind");
+    if (!std::isfinite(s[i].cx) || !std::isfinite(s[i].cy) || !std::isfinite(s[i].rate) ||
+        !(s[i].radius >= 0) || !std::isfinite(s[i].radius))
+      return fail(g, TWS_ERR_INVALID, "non-finite source");
+    if (s[i].kind == TWS_SOURCE_BRUSH && !(s[i].radius > 0))
+      return fail(g, TWS_ERR_INVALID, "brush size must be positive");
+    if (std::fabs(s[i].cx) > 1e8f || std::fabs(s[i].cy) > 1e8f || s[i].radius > 1e8f)
+      return fail(g, TWS_ERR_INVALID, "source out of range");
+  }
+  for (int i = 0; i < n; ++i) g->src[i] = s[i];
+  g->nsrc = n;
+  return TWS_OK;
+}
+
+TWS_API int tws_apply_source(tws_grid* g, const tws_source* s) {
+  if (!g || !s) return fail(g, TWS_ERR_INVALID, "null source");
+  if (s->kind != TWS_SOURCE_DISK && s->kind != TWS_SOURCE_BRUSH) return fail(g, TWS_ERR_INVALID, "bad source kind");
+  if (!std::isfinite(s->cx) || !std::isfinite(s->cy) || !std::isfinite(s->rate) ||
+      !(s->radius >= 0) || std::fabs(s->cx) > 1e8f || std::fabs(s->cy) > 1e8f || s->radius > 1e8f)
+    return fail(g, TWS_ERR_INVALID, "bad source");
+  if (s->kind == TWS_SOURCE_BRUSH && !(s->radius > 0)) return fail(g, TWS_ERR_INVALID, "brush size must be positive");
+  TWS_CUDA(g, launch_apply_source(g->d[g->cur], g->W, g->H, g->pitch, make_dev_source(*s), g->stream),
+           "source kernel");
+  return TWS_OK;
+}
+
+TWS_API int tws_set_steps_per_launch(tws_grid* g, int k) {
+  if (!g || k < 0 || k > 4) return fail(g, TWS_ERR_INVALID, "steps per launch must be 0..4");
+  g->steps_per_launch = k;
+  return TWS_OK;
+}
+
+TWS_API int tws_step(tws_grid* g, int nsteps) {
+  if (!g || nsteps < 0) return fail(g, TWS_ERR_INVALID, "bad step count");
+  if (nsteps == 0) return TWS_OK;
+  return enqueue_steps(g, nsteps);
+}
+
+TWS_API int tws_volume(tws_grid* g, double* out) {
+  if (!g || !out) return fail(g, TWS_ERR_INVALID, "null output");
+  TWS_CUDA(g, launch_volume(g->d[g->cur], g->W, g->H, g->pitch, (double)g->params.cell_area,
+                            g->vol_partials, volume_partials_needed(), g->vol_out, g->stream),
+           "volume kernels");
+  TWS_CUDA(g, cudaMemcpyAsync(g->vol_host, g->vol_out, sizeof(double), cudaMemcpyDeviceToHost, g->stream),
+           "volume copy");
+  TWS_CUDA(g, cudaStreamSynchronize(g->stream), "volume");
+  *out = *g->vol_host;
+  return TWS_OK;
+}
+
+TWS_API int tws_download(tws_grid* g, float* d, float* f, float* v) {
+  if (!g) return TWS_ERR_INVALID;
+  const size_t row = (size_t)g->W * 4, pitch = (size_t)g->pitch * 4;
+  if (d)
+    TWS_CUDA(g, cudaMemcpy2DAsync(d, row, g->d[g->cur], pitch, row, g->H, cudaMemcpyDeviceToHost, g->stream),
+             "download depth");
+  if (f) {
+    if (g->flux_storage == TWS_FLUX_F32) {
+      TWS_CUDA(g, cudaMemcpy2DAsync(f, (size_t)g->W * 16, g->f[g->cur], (size_t)g->pitch * 16,
+                                    (size_t)g->W * 16, g->H, cudaMemcpyDeviceToHost, g->stream),
+               "download flux");
+    } else {
+      float* tmp = nullptr;
+      TWS_CUDA(g, cudaMallocAsync(&tmp, (size_t)g->W * g->H * 16, g->stream), "flux staging");
+      launch_flux_to_f32(g->f[g->cur], g->flux_storage, 1.0f / g->flux_scale, g->W, g->H, g->pitch, tmp,
+                         g->stream);
+      cudaMemcpyAsync(f, tmp, (size_t)g->W * g->H * 16, cudaMemcpyDeviceToHost, g->stream);
+      cudaFreeAsync(tmp, g->stream);
+    }
+  }
+  if (v)
+    TWS_CUDA(g, cudaMemcpy2DAsync(v, (size_t)g->W * 8, g->v, (size_t)g->pitch * 8, (size_t)g->W * 8,
+                                  g->H, cudaMemcpyDeviceToHost, g->stream),
+             "download velocity");
+  TWS_CUDA(g, cudaStreamSynchronize(g->stream), "download");
+  return TWS_OK;
+}
+
+TWS_API int tws_download_terrain(tws_grid* g, float* b) {
+  if (!g || !b) return TWS_ERR_INVALID;
+  const size_t row = (size_t)g->W * 4, pitch = (size_t)g->pitch * 4;
+  TWS_CUDA(g, cudaMemcpy2DAsync(b, row, g->b, pitch, row, g->H, cudaMemcpyDeviceToHost, g->stream),
+           "download terrain");
+  TWS_CUDA(g, cudaStreamSynchronize(g->stream), "download terrain");
+  return TWS_OK;
+}
+
+TWS_API int tws_get_buffers(tws_grid* g, tws_buffers* out) {
+  if (!g || !out) return TWS_ERR_INVALID;
+  out->terrain = g->b;
+  out->depth = g->d[g->cur];
+  out->flux = g->f[g->cur];
+  out->velocity = reinterpret_cast<const float*>(g->v);
+  out->width = g->W;
+  out->height = g->H;
+  out->pitch = g->pitch;
+  out->flux_storage = g->flux_storage;
+  out->flux_scale = g->flux_scale;
+  return TWS_OK;
+}
+
+TWS_API int tws_sync(tws_grid* g) {
+  if (!g) return TWS_ERR_INVALID;
+  TWS_CUDA(g, cudaMemcpyAsync(g->err_host, g->err, sizeof(int), cudaMemcpyDeviceToHost, g->stream),
+           "error word copy");
+  TWS_CUDA(g, cudaStreamSynchronize(g->stream), "sync");
+  if (*g->err_host != kDevErrNone)
+    return fail(g, TWS_ERR_TIMEOUT, "a kernel gave up waiting for its tile loads");
+  return TWS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,79 @@
+// tws_internal.h -- shared declarations of the libtws implementation.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/tws.h"
+
+namespace tws {
+
+// ---------------------------------------------------------------------------
+// Per-step source in the form the kernels read (bounding box precomputed).
+struct DevSource {
+  int kind;
+  float cx, cy, radius, rate;
+  int icx, icy, ir;    // DISK: integer centre and radius
+  int bx0, by0, bx1, by1;  // inclusive bounding box of the cells it can touch
+};
+
+// Everything a step launch needs besides the tensor maps.
+struct StepArgs {
+  int W, H, pitch;
+  float kf, ka, c;
+  int closed;
+  int nsrc;
+  DevSource src[TWS_MAX_SOURCES];
+  float* d_out;
+  void* f_out;
+  float2* v_out;
+  float flux_scale;      // F16 storage: stored = f * flux_scale
+  float flux_inv_scale;  // F16 storage: f = stored * flux_inv_scale
+  int* err;              // device error word (bounded-wait time-outs)
+};
+
+// Kernel variants (temporal block depth K x tile).
+struct StepVariant {
+  int k;      // steps per launch
+  int tx, ty; // interior tile
+  int hx;     // x halo of the b/d boxes (2K rounded up to 4 floats)
+  int bw, bh; // b/d box
+  int fw, fh; // flux box
+  size_t smem;
+};
+
+// Device error codes written to StepArgs::err.
+enum : int { kDevErrNone = 0, kDevErrWaitTimeout = 1 };
+
+// Host helpers implemented in tws_step.cu.
+int step_variant_count();
+const StepVariant& step_variant(int i);
+int step_variant_for(int k, int flux_storage);
+cudaError_t launch_step(int variant, int flux_storage, const CUtensorMap& tm_b,
+                        const CUtensorMap& tm_d, const CUtensorMap& tm_f, const StepArgs& a,
+                        cudaStream_t s);
+cudaError_t encode_step_maps(int variant, int flux_storage, int W, int H, int pitch,
+                             const float* b, const float* d, const void* f, CUtensorMap* tm_b,
+                             CUtensorMap* tm_d, CUtensorMap* tm_f, std::string* why);
+
+// tws_aux.cu
+cudaError_t launch_apply_source(float* d, int W, int H, int pitch, const DevSource& s,
+                                cudaStream_t st);
+cudaError_t launch_volume(const float* d, int W, int H, int pitch, double cell_area,
+                          double* partials, int max_partials, double* out, cudaStream_t st);
+int volume_partials_needed();
+cudaError_t launch_generate_scene(uint64_t seed, int W, int H, int pitch, float height_scale,
+                                  float fill, float* b, float* d, cudaStream_t st);
+cudaError_t launch_flux_to_f32(const void* f, int flux_storage, float inv_scale, int W, int H,
+                               int pitch, float* out_packed, cudaStream_t st);
+cudaError_t launch_flux_from_f32(const float* in_packed, int flux_storage, float scale, int W,
+                                 int H, int pitch, void* f, cudaStream_t st);
+
+DevSource make_dev_source(const tws_source& s);
+void count_launch(uint64_t n = 1);
+
+}  // namespace tws

@@ -1,0 +1,476 @@
+// tws_step.cu -- the fused virtual-pipe step kernel for sm_103a.
+//
+// One launch advances a grid by K steps (K = 1: the plain kernel; K > 1:
+// temporal blocking).  Per step and per cell it computes, in the reference's
+// operation order:
+//   source term              waterBrush.comp:26-28 / the benchmark's rain disk
+//   outflow flux + scaling   flowUpdate.comp:34-62
+//   depth update, flow map   flowApply.comp:32-52
+// The two reference dispatches (Terrain.cpp:253-265) become one kernel: a CTA
+// owns a TX x TY tile of output cells, loads b and d with a 2K-cell halo and
+// the flux with a (2K-1)-cell halo into shared memory with TMA
+// (cp.async.bulk.tensor, completion on an mbarrier), recomputes the halo
+// fluxes it needs, and writes d, f and the flow map of its tile once.
+// The halo cells are recomputed redundantly by neighbouring CTAs, so there is
+// no inter-CTA dependency inside a launch.
+//
+// Arithmetic is IEEE round-to-nearest with no contraction (__fmul_rn etc.),
+// so the result is bit-identical to the FP32 CPU transcription of the shaders.
+//
+// HBM layout (per grid): b, d[2] float with a row pitch that is a multiple of
+// 32 elements; f[2] float4 (or 4 x half) per cell, same pitch; v float2.
+
+#include <cudaTypedefs.h>
+
+#include <cstdio>
+#include <mutex>
+
+#include "tws_device.cuh"
+#include "tws_internal.h"
+
+namespace tws {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr long long kWaitCycles = 4000000000LL;  // bounded-wait limit in SM clocks
+
+// ---- shared memory / TMA / mbarrier primitives -----------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int c0, int c1,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tm, int c0, int c1,
+                                            int c2, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Bounded wait on phase `parity`: gives up after kWaitCycles SM clocks (about
+// two seconds; a tile load takes microseconds).  On time-out: record the
+// error, wait once more (bounded) so no copy is left writing into shared
+// memory, report false.
+__device__ bool wait_bounded(uint64_t* bar, uint32_t parity, int* err) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity)) {
+    if (clock64() - t0 > kWaitCycles) {
+      if (threadIdx.x == 0) atomicExch(err, kDevErrWaitTimeout);
+      const long long t1 = clock64();
+      while (!mbar_try_wait(bar, parity) && clock64() - t1 < kWaitCycles) {
+      }
+      return false;
+    }
+  }
+  return true;
+}
+
+// ---- tile geometry -----------------------------------------------------------
+__host__ __device__ constexpr size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+template <int K, int TX, int TY, bool F16>
+struct Tile {
+  static constexpr int HX = (2 * K + 3) / 4 * 4;  // x halo of b/d, whole 16-byte units
+  static constexpr int HY = 2 * K;                // y halo of b/d
+  static constexpr int BW = TX + 2 * HX, BH = TY + 2 * HY;
+  static constexpr int RF = 2 * K - 1;  // flux halo
+  static constexpr int FW = TX + 2 * RF, FH = TY + 2 * RF;
+  static constexpr int SW = FW + 2;  // F16 staging width in cells (starts one cell early)
+  static constexpr int NB = BW * BH, NF = FW * FH;
+  static constexpr size_t OFF_B = 0;
+  static constexpr size_t OFF_D = align_up(OFF_B + NB * 4, 128);
+  static constexpr size_t OFF_H = align_up(OFF_D + NB * 4, 128);
+  static constexpr size_t OFF_F = align_up(OFF_H + NB * 4, 128);
+  static constexpr size_t OFF_S = align_up(OFF_F + (size_t)NF * 16, 128);
+  static constexpr size_t OFF_BAR = align_up(OFF_S + (F16 ? (size_t)SW * FH * 8 : 0), 128);
+  static constexpr size_t SMEM = OFF_BAR + 16 + 128;  // + slack to align the base
+  static constexpr uint32_t TX_BYTES =
+      (uint32_t)(2 * NB * 4 + (F16 ? SW * FH * 8 : NF * 16));
+};
+
+// F16 storage rounding: the value the next step will read back.
+__device__ __forceinline__ float quantize_f16(float v, float scale, float inv_scale) {
+  const float s = fminf(fmul(v, scale), 65504.0f);
+  return fmul(__half2float(__float2half_rn(s)), inv_scale);
+}
+
+// ---- the kernel --------------------------------------------------------------
+template <int K, int TX, int TY, bool F16>
+__global__ void __launch_bounds__(kThreads)
+    step_kernel(const __grid_constant__ CUtensorMap tm_b, const __grid_constant__ CUtensorMap tm_d,
+                const __grid_constant__ CUtensorMap tm_f, const __grid_constant__ StepArgs a) {
+  using T = Tile<K, TX, TY, F16>;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~static_cast<uintptr_t>(127));
+  float* sb = reinterpret_cast<float*>(smem + T::OFF_B);
+  float* sd = reinterpret_cast<float*>(smem + T::OFF_D);
+  float* sh = reinterpret_cast<float*>(smem + T::OFF_H);
+  float4* sf = reinterpret_cast<float4*>(smem + T::OFF_F);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + T::OFF_BAR);
+
+  const int tid = threadIdx.x;
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+  const int W = a.W, H = a.H;
+
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    mbar_expect_tx(bar, T::TX_BYTES);
+    tma_load_2d(sb, &tm_b, x0 - T::HX, y0 - T::HY, bar);
+    tma_load_2d(sd, &tm_d, x0 - T::HX, y0 - T::HY, bar);
+    if (F16) {
+      // cell pairs; x0 - RF - 1 = x0 - 2K is even
+      tma_load_3d(smem + T::OFF_S, &tm_f, 0, (x0 - T::RF - 1) / 2, y0 - T::RF, bar);
+    } else {
+      tma_load_3d(sf, &tm_f, 0, x0 - T::RF, y0 - T::RF, bar);
+    }
+  }
+
+  // Which sources can touch this CTA's b/d box.
+  uint32_t mask = 0;
+#pragma unroll
+  for (int k = 0; k < TWS_MAX_SOURCES; ++k) {
+    if (k < a.nsrc) {
+      const DevSource& s = a.src[k];
+      if (s.bx1 >= x0 - T::HX && s.bx0 < x0 + TX + T::HX && s.by1 >= y0 - T::HY &&
+          s.by0 < y0 + TY + T::HY)
+        mask |= 1u << k;
+    }
+  }
+
+  if (!wait_bounded(bar, 0, a.err)) return;
+
+  // Phase 0: first step's sources, surface height h = d + b (flowUpdate.comp:34).
+  for (int idx = tid; idx < T::NB; idx += kThreads) {
+    float d = sd[idx];
+    if (mask) {
+      const int i = idx / T::BW, j = idx - (idx / T::BW) * T::BW;
+      const int gx = x0 - T::HX + j, gy = y0 - T::HY + i;
+      if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+        d = add_sources(d, gx, gy, a, mask);
+        sd[idx] = d;
+      }
+    }
+    sh[idx] = fadd(d, sb[idx]);
+  }
+  if (F16) {
+    const __half2* st = reinterpret_cast<const __half2*>(smem + T::OFF_S);
+    for (int idx = tid; idx < T::NF; idx += kThreads) {
+      const int i = idx / T::FW, j = idx - (idx / T::FW) * T::FW;
+      const int s = i * T::SW + j + 1;
+      const float2 lo = __half22float2(st[2 * s]), hi = __half22float2(st[2 * s + 1]);
+      sf[idx] = make_float4(fmul(lo.x, a.flux_inv_scale), fmul(lo.y, a.flux_inv_scale),
+                            fmul(hi.x, a.flux_inv_scale), fmul(hi.y, a.flux_inv_scale));
+    }
+  }
+  __syncthreads();
+
+#pragma unroll
+  for (int s = 0; s < K; ++s) {
+    const int rf = T::RF - 2 * s;  // ring of flux computed in this step
+    const int rd = rf - 1;         // ring of depth computed in this step
+
+    // Phase A: outflow flux with non-negativity scaling, flowUpdate.comp:34-62.
+    {
+      const int RW = TX + 2 * rf, RH = TY + 2 * rf;
+      for (int idx = tid; idx < RW * RH; idx += kThreads) {
+        const int i = idx / RW, j = idx - (idx / RW) * RW;
+        const int fi = T::RF - rf + i, fj = T::RF - rf + j;
+        const int gx = x0 - T::RF + fj, gy = y0 - T::RF + fi;
+        if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
+        const int bidx = (fi + T::HY - T::RF) * T::BW + (fj + T::HX - T::RF);
+        const float hc = sh[bidx];
+        const float ex1 = fsub(hc, sh[bidx + 1]);
+        const float ex0 = fsub(hc, sh[bidx - 1]);
+        const float ey1 = fsub(hc, sh[bidx + T::BW]);
+        const float ey0 = fsub(hc, sh[bidx - T::BW]);
+        const float dc = sd[bidx];
+        const int fidx = fi * T::FW + fj;
+        const float4 fo = sf[fidx];
+        float4 nf;
+        nf.x = max0(fadd(fmul(fo.x, a.kf), fmul(ex1, a.ka)));
+        nf.y = max0(fadd(fmul(fo.y, a.kf), fmul(ex0, a.ka)));
+        nf.z = max0(fadd(fmul(fo.z, a.kf), fmul(ey1, a.ka)));
+        nf.w = max0(fadd(fmul(fo.w, a.kf), fmul(ey0, a.ka)));
+        if (a.closed) {
+          if (gx + 1 >= W) nf.x = 0.0f;
+          if (gx == 0) nf.y = 0.0f;
+          if (gy + 1 >= H) nf.z = 0.0f;
+          if (gy == 0) nf.w = 0.0f;
+        }
+        const float total = fmul(fadd(fadd(fadd(nf.x, nf.y), nf.z), nf.w), a.c);
+        if (total > dc) {
+          const float sc = fdiv(dc, total);
+          nf.x = fmul(nf.x, sc);
+          nf.y = fmul(nf.y, sc);
+          nf.z = fmul(nf.z, sc);
+          nf.w = fmul(nf.w, sc);
+        }
+        if (F16) {
+          nf.x = quantize_f16(nf.x, a.flux_scale, a.flux_inv_scale);
+          nf.y = quantize_f16(nf.y, a.flux_scale, a.flux_inv_scale);
+          nf.z = quantize_f16(nf.z, a.flux_scale, a.flux_inv_scale);
+          nf.w = quantize_f16(nf.w, a.flux_scale, a.flux_inv_scale);
+        }
+        sf[fidx] = nf;
+      }
+    }
+    __syncthreads();
+
+    // Phase B: depth update and flow vector, flowApply.comp:32-52.
+    {
+      const int RW = TX + 2 * rd, RH = TY + 2 * rd;
+      for (int idx = tid; idx < RW * RH; idx += kThreads) {
+        const int i = idx / RW, j = idx - (idx / RW) * RW;
+        const int fi = T::RF - rd + i, fj = T::RF - rd + j;
+        const int gx = x0 - T::RF + fj, gy = y0 - T::RF + fi;
+        if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
+        const int fidx = fi * T::FW + fj;
+        const float4 fc = sf[fidx];
+        const float X1 = sf[fidx + 1].y;       // -x outflow of the +x neighbour
+        const float X0 = sf[fidx - 1].x;       // +x outflow of the -x neighbour
+        const float Y1 = sf[fidx + T::FW].w;   // -y outflow of the +y neighbour
+        const float Y0 = sf[fidx - T::FW].z;   // +y outflow of the -y neighbour
+        const int bidx = (fi + T::HY - T::RF) * T::BW + (fj + T::HX - T::RF);
+        const float in = fadd(fadd(fadd(X1, X0), Y1), Y0);
+        const float out = fadd(fadd(fadd(fc.x, fc.y), fc.z), fc.w);
+        const float dn = max0(fadd(sd[bidx], fmul(fsub(in, out), a.c)));
+        if (s == K - 1) {
+          const size_t g = (size_t)gy * a.pitch + gx;
+          a.d_out[g] = dn;
+          if (F16) {
+            const __half2 lo = __floats2half2_rn(fmul(fc.x, a.flux_scale), fmul(fc.y, a.flux_scale));
+            const __half2 hi = __floats2half2_rn(fmul(fc.z, a.flux_scale), fmul(fc.w, a.flux_scale));
+            uint2 packed;
+            packed.x = *reinterpret_cast<const uint32_t*>(&lo);
+            packed.y = *reinterpret_cast<const uint32_t*>(&hi);
+            reinterpret_cast<uint2*>(a.f_out)[g] = packed;
+          } else {
+            reinterpret_cast<float4*>(a.f_out)[g] = fc;
+          }
+          a.v_out[g] = make_float2(fsub(fsub(X1, fc.x), fsub(X0, fc.y)),
+                                   fsub(fsub(Y1, fc.z), fsub(Y0, fc.w)));
+        } else {
+          const float dnext = mask ? add_sources(dn, gx, gy, a, mask) : dn;
+          sd[bidx] = dnext;
+          sh[bidx] = fadd(dnext, sb[bidx]);
+        }
+      }
+    }
+    if (s < K - 1) __syncthreads();
+  }
+}
+
+// ---- variant table -------------------------------------------------------------
+using KernelFn = void (*)(CUtensorMap, CUtensorMap, CUtensorMap, StepArgs);
+
+struct VariantEntry {
+  StepVariant v;
+  const void* fn32;
+  const void* fn16;
+};
+
+template <int K, int TX, int TY>
+VariantEntry make_entry() {
+  using T = Tile<K, TX, TY, true>;
+  using T32 = Tile<K, TX, TY, false>;
+  VariantEntry e;
+  e.v.k = K;
+  e.v.tx = TX;
+  e.v.ty = TY;
+  e.v.hx = T32::HX;
+  e.v.bw = T32::BW;
+  e.v.bh = T32::BH;
+  e.v.fw = T32::FW;
+  e.v.fh = T32::FH;
+  e.v.smem = T::SMEM;  // the larger of the two
+  e.fn32 = reinterpret_cast<const void*>(&step_kernel<K, TX, TY, false>);
+  e.fn16 = reinterpret_cast<const void*>(&step_kernel<K, TX, TY, true>);
+  return e;
+}
+
+template <int K, int TX, int TY>
+size_t smem_of(bool f16) {
+  return f16 ? Tile<K, TX, TY, true>::SMEM : Tile<K, TX, TY, false>::SMEM;
+}
+
+struct VariantTable {
+  VariantEntry e[8];
+  size_t smem32[8], smem16[8];
+  int n = 0;
+  bool attr_set32[8] = {}, attr_set16[8] = {};
+  std::mutex mu;
+  VariantTable() {
+    add<1, 64, 16>();
+    add<1, 64, 32>();
+    add<2, 64, 32>();
+    add<3, 64, 32>();
+    add<4, 64, 32>();
+    add<4, 64, 48>();
+  }
+  template <int K, int TX, int TY>
+  void add() {
+    e[n] = make_entry<K, TX, TY>();
+    smem32[n] = smem_of<K, TX, TY>(false);
+    smem16[n] = smem_of<K, TX, TY>(true);
+    ++n;
+  }
+};
+
+VariantTable& table() {
+  static VariantTable t;
+  return t;
+}
+
+using EncodeTiledFn = PFN_cuTensorMapEncodeTiled_v12000;
+
+EncodeTiledFn encode_fn(std::string* why) {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  static cudaError_t err = cudaSuccess;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    err = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
+    if (err == cudaSuccess && q == cudaDriverEntryPointSuccess) fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  if (!fn && why) *why = "cuTensorMapEncodeTiled is not available from the driver";
+  return fn;
+}
+
+}  // namespace
+
+int step_variant_count() { return table().n; }
+const StepVariant& step_variant(int i) { return table().e[i].v; }
+
+int step_variant_for(int k, int /*flux_storage*/) {
+  // Default tile per temporal depth.
+  switch (k) {
+    case 1: return 1;  // K=1, 64x32
+    case 2: return 2;
+    case 3: return 3;
+    case 4: return 4;
+    default: return -1;
+  }
+}
+
+cudaError_t encode_step_maps(int variant, int flux_storage, int W, int H, int pitch,
+                             const float* b, const float* d, const void* f, CUtensorMap* tm_b,
+                             CUtensorMap* tm_d, CUtensorMap* tm_f, std::string* why) {
+  EncodeTiledFn enc = encode_fn(why);
+  if (!enc) return cudaErrorNotSupported;
+  const StepVariant& v = step_variant(variant);
+  const cuuint32_t estr[3] = {1, 1, 1};
+  // b and d: 2-D float {W, H}.
+  const cuuint64_t gdim2[2] = {(cuuint64_t)W, (cuuint64_t)H};
+  const cuuint64_t gstr2[1] = {(cuuint64_t)pitch * 4};
+  const cuuint32_t box2[2] = {(cuuint32_t)v.bw, (cuuint32_t)v.bh};
+  CUresult r;
+  if (b) {
+    r = enc(tm_b, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(b), gdim2, gstr2, box2,
+            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+      if (why) *why = "tensor map for terrain failed, CUresult " + std::to_string((int)r);
+      return cudaErrorInvalidValue;
+    }
+  }
+  if (d) {
+    r = enc(tm_d, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(d), gdim2, gstr2, box2,
+            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+      if (why) *why = "tensor map for depth failed, CUresult " + std::to_string((int)r);
+      return cudaErrorInvalidValue;
+    }
+  }
+  if (f) {
+    if (flux_storage == TWS_FLUX_F32) {
+      // 3-D float {4 channels, W, H}: one 16-byte record per cell.
+      const cuuint64_t gdim[3] = {4, (cuuint64_t)W, (cuuint64_t)H};
+      const cuuint64_t gstr[2] = {16, (cuuint64_t)pitch * 16};
+      const cuuint32_t box[3] = {4, (cuuint32_t)v.fw, (cuuint32_t)v.fh};
+      r = enc(tm_f, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(f), gdim, gstr, box,
+              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    } else {
+      // 3-D half {8 = two cells x 4 channels, ceil(W/2) cell pairs, H}.  The
+      // box starts one cell before the flux halo so its x coordinate is whole
+      // pairs; the padding cell of an odd-width row is kept at zero.
+      const cuuint64_t gdim[3] = {8, (cuuint64_t)((W + 1) / 2), (cuuint64_t)H};
+      const cuuint64_t gstr[2] = {16, (cuuint64_t)pitch * 8};
+      const cuuint32_t box[3] = {8, (cuuint32_t)((v.fw + 2) / 2), (cuuint32_t)v.fh};
+      r = enc(tm_f, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, const_cast<void*>(f), gdim, gstr, box,
+              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    }
+    if (r != CUDA_SUCCESS) {
+      if (why) *why = "tensor map for flux failed, CUresult " + std::to_string((int)r);
+      return cudaErrorInvalidValue;
+    }
+  }
+  return cudaSuccess;
+}
+
+cudaError_t launch_step(int variant, int flux_storage, const CUtensorMap& tm_b,
+                        const CUtensorMap& tm_d, const CUtensorMap& tm_f, const StepArgs& a,
+                        cudaStream_t s) {
+  VariantTable& t = table();
+  if (variant < 0 || variant >= t.n) return cudaErrorInvalidValue;
+  const bool f16 = flux_storage == TWS_FLUX_F16;
+  const void* fn = f16 ? t.e[variant].fn16 : t.e[variant].fn32;
+  const size_t smem = f16 ? t.smem16[variant] : t.smem32[variant];
+  {
+    std::lock_guard<std::mutex> lk(t.mu);
+    bool& set = f16 ? t.attr_set16[variant] : t.attr_set32[variant];
+    if (!set) {
+      cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      set = true;
+    }
+  }
+  const StepVariant& v = t.e[variant].v;
+  dim3 grid((a.W + v.tx - 1) / v.tx, (a.H + v.ty - 1) / v.ty);
+  auto kfn = reinterpret_cast<KernelFn>(const_cast<void*>(fn));
+  kfn<<<grid, kThreads, smem, s>>>(tm_b, tm_d, tm_f, a);
+  count_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace tws

@@ -1,0 +1,68 @@
+"""The C++ facade (include/tws_watersim.hpp) used from a C++ program the way
+the reference's scene uses Terrain: frame-time driven PerformSimulationStep
+with its 10-step clamp, brush strokes, parameter setters.  The program is
+compiled here against libtws.so and its output compared with the oracle."""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, assert_bitexact
+
+pytestmark = pytest.mark.gpu
+
+
+def _build(tmp_path):
+    import terrainwatersim_gb300 as tws
+    lib_dir = os.path.dirname(tws.library_path())
+    exe = str(tmp_path / "facade_check")
+    cxx = shutil.which("g++") or "g++"
+    subprocess.run([cxx, "-std=c++17", "-O2", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "facade_check.cpp"), "-L", lib_dir, "-ltws",
+                    f"-Wl,-rpath,{lib_dir}", "-o", exe], check=True)
+    return exe
+
+
+def test_cpp_facade_matches_oracle(tmp_path, oracle):
+    N = 128
+    exe = _build(tmp_path)
+    out = str(tmp_path / "state.bin")
+    r = subprocess.run([exe, str(N), out], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    raw = np.fromfile(out, dtype=np.uint8)
+    total = int(raw[:4].view(np.uint32)[0])
+    body = raw[4:].view(np.float32)
+    d = body[:N * N].reshape(N, N)
+    f = body[N * N:5 * N * N].reshape(N, N, 4)
+    v = body[5 * N * N:].reshape(N, N, 2)
+
+    # replay: Terrain.cpp:242-247 accumulator in double, step 1/60 s as float
+    step = float(np.float32(1.0) / np.float32(60.0))
+    acc, steps = 0.0, []
+    for fr in (0.025, 0.025, 0.4, 0.025, 0.010, 0.030):
+        acc += fr
+        n = int(acc / step)
+        acc -= step * n
+        steps.append(min(n, 10))
+    assert total == sum(steps)
+    kf, ka, c = oracle.params_reference(60.0, 0.97, 20.0, float(N), N)
+    b, od = oracle.terrain(77, N, N, 40.0, 15.0)
+    of = np.zeros((N, N, 4), np.float32)
+    ov = np.zeros((N, N, 2), np.float32)
+    wx = np.float32(np.float32(0.3) * np.float32(N)) + np.float32(np.float32(5.0) * np.float32(N))
+    wz = np.float32(np.float32(0.6) * np.float32(N))
+    px, pz = np.float32(wx / np.float32(N)), np.float32(wz / np.float32(N))
+    px, pz = np.float32(px - np.trunc(px)), np.float32(pz - np.trunc(pz))
+    bx, by = float(np.float32(px * np.float32(N))), float(np.float32(pz * np.float32(N)))
+    for i, n in enumerate(steps):
+        if i == 1:
+            oracle.sources_f32(od, [(oracle.SOURCE_BRUSH, bx, by, 32.0, 4.0)])
+        if n:
+            oracle.step_f32(b, od, of, ov, kf, ka, c, oracle.BOUNDARY_OPEN, nsteps=n)
+    assert_bitexact(d, od, "depth")
+    assert_bitexact(f, of, "flux")
+    assert_bitexact(v, ov, "velocity")

@@ -158,6 +158,25 @@ TWS_API int tws_apply_source(tws_grid* grid, const tws_source* source);
  * not depend on it (bit-identical). */
 TWS_API int tws_set_steps_per_launch(tws_grid* grid, int steps_per_launch);
 
+/* Kernel variants: each is a temporal depth K (steps per launch) and an
+ * output tile.  tws_variant_info describes variant i (any pointer may be
+ * NULL); returns TWS_ERR_INVALID past the last one. */
+TWS_API int tws_variant_count(void);
+TWS_API int tws_variant_info(int variant, int* steps_per_launch, int* tile_x, int* tile_y,
+                             size_t* shared_bytes);
+
+/* Pin a variant for this grid (-1: automatic -- the tuned choice for this
+ * grid shape if tws_autotune ran for one, else the steps-per-launch setting). */
+TWS_API int tws_set_variant(tws_grid* grid, int variant);
+
+/* Autotuner: times every variant for `trial_steps` steps on this grid's
+ * current state (restored afterwards, so the simulation is unchanged), picks
+ * the fastest per cell-step, pins it on this grid and records it for every
+ * later grid of the same width, height and flux storage in this process.
+ * Synchronous.  `chosen` (may be NULL) receives the variant index.  No
+ * counterpart in the reference. */
+TWS_API int tws_autotune(tws_grid* grid, int trial_steps, int* chosen);
+
 /* Advance `nsteps` steps: per step, sources, then the outflow update with
  * non-negativity scaling (flowUpdate.comp:12-63), then the depth update and
  * flow vector (flowApply.comp:13-53), fused.  Replaces the dispatch loop of

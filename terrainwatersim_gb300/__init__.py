@@ -21,7 +21,7 @@ import numpy as np
 
 __all__ = [
     "TwsError", "SimParams", "Source", "Buffers", "Grid", "lib", "library_path",
-    "params_physical", "params_reference", "rain_disks",
+    "params_physical", "params_reference", "rain_disks", "variants",
     "BOUNDARY_CLOSED", "BOUNDARY_OPEN", "FLUX_F32", "FLUX_F16", "SOURCE_DISK", "SOURCE_BRUSH",
     "MAX_SOURCES",
 ]
@@ -96,6 +96,10 @@ def _declare(L):
         "tws_set_sources": ([vp, vp, i], i),
         "tws_apply_source": ([vp, vp], i),
         "tws_set_steps_per_launch": ([vp, i], i),
+        "tws_variant_count": ([], i),
+        "tws_variant_info": ([i, vp, vp, vp, vp], i),
+        "tws_set_variant": ([vp, i], i),
+        "tws_autotune": ([vp, i, vp], i),
         "tws_step": ([vp, i], i),
         "tws_volume": ([vp, vp], i),
         "tws_download": ([vp, vp, vp, vp], i),
@@ -157,6 +161,17 @@ def rain_disks(seed: int, width: int, height: int, radius: int, rate: float, cou
     arr = (Source * max(1, count))()
     _check(lib().tws_scene_rain_disks(seed, width, height, radius, rate, count, arr))
     return [(s.kind, s.cx, s.cy, s.radius, s.rate) for s in arr[:count]]
+
+
+def variants():
+    """[(steps_per_launch, tile_x, tile_y, shared_bytes)] of the step kernel."""
+    L = lib()
+    out = []
+    for i in range(L.tws_variant_count()):
+        k, tx, ty, sm = C.c_int(), C.c_int(), C.c_int(), C.c_size_t()
+        _check(L.tws_variant_info(i, C.byref(k), C.byref(tx), C.byref(ty), C.byref(sm)))
+        out.append((k.value, tx.value, ty.value, sm.value))
+    return out
 
 
 def _host_f32(a, shape):
@@ -239,6 +254,16 @@ class Grid:
 
     def set_steps_per_launch(self, k: int):
         _check(lib().tws_set_steps_per_launch(self._h, k), self._h)
+
+    def set_variant(self, variant: int):
+        _check(lib().tws_set_variant(self._h, variant), self._h)
+
+    def autotune(self, trial_steps: int = 24) -> int:
+        """Time every kernel variant on this grid's state (restored after)
+        and pin the fastest; returns its index."""
+        out = C.c_int()
+        _check(lib().tws_autotune(self._h, trial_steps, C.byref(out)), self._h)
+        return out.value
 
     def step(self, nsteps: int = 1):
         _check(lib().tws_step(self._h, nsteps), self._h)

@@ -331,18 +331,24 @@ size_t smem_of(bool f16) {
 }
 
 struct VariantTable {
-  VariantEntry e[8];
-  size_t smem32[8], smem16[8];
+  VariantEntry e[16];
+  size_t smem32[16], smem16[16];
   int n = 0;
-  bool attr_set32[8] = {}, attr_set16[8] = {};
+  bool attr_set32[16] = {}, attr_set16[16] = {};
   std::mutex mu;
   VariantTable() {
-    add<1, 64, 16>();
-    add<1, 64, 32>();
-    add<2, 64, 32>();
-    add<3, 64, 32>();
-    add<4, 64, 32>();
-    add<4, 64, 48>();
+    // index: K, tile -- the first entry of each K is its default
+    add<1, 64, 32>();   // 0
+    add<2, 64, 32>();   // 1
+    add<3, 64, 32>();   // 2
+    add<4, 64, 32>();   // 3
+    add<1, 64, 16>();   // 4
+    add<1, 128, 16>();  // 5
+    add<1, 32, 32>();   // 6
+    add<1, 64, 8>();    // 7
+    add<2, 128, 16>();  // 8
+    add<2, 64, 16>();   // 9
+    add<4, 64, 48>();   // 10
   }
   template <int K, int TX, int TY>
   void add() {
@@ -380,14 +386,8 @@ int step_variant_count() { return table().n; }
 const StepVariant& step_variant(int i) { return table().e[i].v; }
 
 int step_variant_for(int k, int /*flux_storage*/) {
-  // Default tile per temporal depth.
-  switch (k) {
-    case 1: return 1;  // K=1, 64x32
-    case 2: return 2;
-    case 3: return 3;
-    case 4: return 4;
-    default: return -1;
-  }
+  // Default tile per temporal depth: the first table entry with that K.
+  return (k >= 1 && k <= 4) ? k - 1 : -1;
 }
 
 cudaError_t encode_step_maps(int variant, int flux_storage, int W, int H, int pitch,

@@ -101,3 +101,13 @@ def test_binding_raises_when_library_missing(tmp_path, monkeypatch):
     monkeypatch.setattr(t, "_lib", None)
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         t.lib()
+
+
+def test_variant_table(tws):
+    v = tws.variants()
+    assert len(v) >= 4
+    assert {k for k, _, _, _ in v} == {1, 2, 3, 4}
+    for k, tx, ty, smem in v:
+        assert tx % 4 == 0 and ty >= 1 and 0 < smem <= 227 * 1024
+    import ctypes as C
+    assert tws.lib().tws_variant_info(len(v), None, None, None, None) == tws.ERR_INVALID

@@ -264,3 +264,48 @@ def test_error_paths(tws):
         g.sync()  # no device-side error after normal work
         buf = g.buffers()
         assert buf.pitch % 32 == 0 and buf.width == 16 and buf.depth
+
+
+# ------------------------------------------------------------ variants and autotuner
+
+@pytest.mark.parametrize("W,H", [(97, 130), (300, 41), (1, 70)])
+def test_every_kernel_variant_bitexact(tws, oracle, W, H):
+    """Every (temporal depth, tile) variant, with a step count that leaves a
+    remainder for the shallower kernels, matches the oracle bit for bit."""
+    rng = np.random.default_rng(W + 7 * H)
+    b = rng.uniform(0, 6, (H, W)).astype(np.float32)
+    d = np.maximum(0, rng.uniform(-2, 5, (H, W))).astype(np.float32)
+    f = rng.uniform(0, 0.3, (H, W, 4)).astype(np.float32)
+    p = tws.params_physical(boundary=tws.BOUNDARY_CLOSED)
+    srcs = [(tws.SOURCE_DISK, W // 3, H // 2, 5, 0.05)]
+    od, of, ov = oracle_run(oracle, b, d, f, p.as_tuple(), srcs, 13, oracle.BOUNDARY_CLOSED)
+    for vi in range(len(tws.variants())):
+        with tws.Grid(W, H, p) as g:
+            g.upload(b, d, f)
+            g.set_sources(srcs)
+            g.set_variant(vi)
+            g.step(13)
+            gd, gf, gv = g.download()
+        assert_bitexact(gd, od, f"depth variant {vi}")
+        assert_bitexact(gf, of, f"flux variant {vi}")
+        assert_bitexact(gv, ov, f"velocity variant {vi}")
+
+
+def test_autotune_preserves_state_and_pins_a_variant(tws, oracle):
+    W, H = 512, 384
+    p = tws.params_physical(boundary=tws.BOUNDARY_CLOSED)
+    rain = tws.rain_disks(3, W, H, 20, 0.01, 1)
+    b, d = oracle.terrain(3, W, H, 40.0, 15.0)
+    with tws.Grid(W, H, p) as g:
+        g.upload(b, d)
+        g.set_sources(rain)
+        g.step(5)
+        best = g.autotune(12)
+        assert 0 <= best < len(tws.variants())
+        g.step(7)
+        gd, gf, gv = g.download()
+    od, of, ov = oracle_run(oracle, b, d, np.zeros((H, W, 4), np.float32), p.as_tuple(), rain, 12,
+                            oracle.BOUNDARY_CLOSED)
+    assert_bitexact(gd, od, "depth")
+    assert_bitexact(gf, of, "flux")
+    assert_bitexact(gv, ov, "velocity")

@@ -338,7 +338,7 @@ def run_ours(args):
             },
             "variants": {
                 (f"{'plain' if vinfo[i][0] == 1 else 'blocked_k%d' % vinfo[i][0]}"
-                 f"_{vinfo[i][1]}x{vinfo[i][2]}"): {
+                 f"_{vinfo[i][1]}x{vinfo[i][2]}_{'persistent' if vinfo[i][3] > 1 else 'pertile'}"): {
                     "variant": i,
                     "gcell_steps_per_s": round(cells * chain * v["steps"] * ws / v["seconds"] / 1e9,
                                                3),

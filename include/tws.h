@@ -158,12 +158,14 @@ TWS_API int tws_apply_source(tws_grid* grid, const tws_source* source);
  * not depend on it (bit-identical). */
 TWS_API int tws_set_steps_per_launch(tws_grid* grid, int steps_per_launch);
 
-/* Kernel variants: each is a temporal depth K (steps per launch) and an
- * output tile.  tws_variant_info describes variant i (any pointer may be
- * NULL); returns TWS_ERR_INVALID past the last one. */
+/* Kernel variants: each is a temporal depth K (steps per launch), an output
+ * tile and a pipeline depth (1: one CTA per tile; 2: persistent CTAs that
+ * prefetch their next tile while computing).  tws_variant_info describes
+ * variant i (any pointer may be NULL); returns TWS_ERR_INVALID past the last
+ * one. */
 TWS_API int tws_variant_count(void);
 TWS_API int tws_variant_info(int variant, int* steps_per_launch, int* tile_x, int* tile_y,
-                             size_t* shared_bytes);
+                             int* stages, size_t* shared_bytes);
 
 /* Pin a variant for this grid (-1: automatic -- the tuned choice for this
  * grid shape if tws_autotune ran for one, else the steps-per-launch setting). */

@@ -97,7 +97,7 @@ def _declare(L):
         "tws_apply_source": ([vp, vp], i),
         "tws_set_steps_per_launch": ([vp, i], i),
         "tws_variant_count": ([], i),
-        "tws_variant_info": ([i, vp, vp, vp, vp], i),
+        "tws_variant_info": ([i, vp, vp, vp, vp, vp], i),
         "tws_set_variant": ([vp, i], i),
         "tws_autotune": ([vp, i, vp], i),
         "tws_step": ([vp, i], i),
@@ -164,13 +164,14 @@ def rain_disks(seed: int, width: int, height: int, radius: int, rate: float, cou
 
 
 def variants():
-    """[(steps_per_launch, tile_x, tile_y, shared_bytes)] of the step kernel."""
+    """[(steps_per_launch, tile_x, tile_y, stages, shared_bytes)] of the step kernel."""
     L = lib()
     out = []
     for i in range(L.tws_variant_count()):
-        k, tx, ty, sm = C.c_int(), C.c_int(), C.c_int(), C.c_size_t()
-        _check(L.tws_variant_info(i, C.byref(k), C.byref(tx), C.byref(ty), C.byref(sm)))
-        out.append((k.value, tx.value, ty.value, sm.value))
+        k, tx, ty, st, sm = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_size_t()
+        _check(L.tws_variant_info(i, C.byref(k), C.byref(tx), C.byref(ty), C.byref(st),
+                                  C.byref(sm)))
+        out.append((k.value, tx.value, ty.value, st.value, sm.value))
     return out
 
 

@@ -418,12 +418,13 @@ TWS_API int tws_set_steps_per_launch(tws_grid* g, int k) {
 
 TWS_API int tws_variant_count(void) { return step_variant_count(); }
 
-TWS_API int tws_variant_info(int i, int* k, int* tx, int* ty, size_t* smem) {
+TWS_API int tws_variant_info(int i, int* k, int* tx, int* ty, int* stages, size_t* smem) {
   if (i < 0 || i >= step_variant_count()) return TWS_ERR_INVALID;
   const StepVariant& v = step_variant(i);
   if (k) *k = v.k;
   if (tx) *tx = v.tx;
   if (ty) *ty = v.ty;
+  if (stages) *stages = v.stages;
   if (smem) *smem = v.smem;
   return TWS_OK;
 }

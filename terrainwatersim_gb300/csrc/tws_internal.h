@@ -40,6 +40,7 @@ struct StepArgs {
 struct StepVariant {
   int k;      // steps per launch
   int tx, ty; // interior tile
+  int stages; // 1: one CTA per tile; 2: persistent CTAs, next tile prefetched
   int hx;     // x halo of the b/d boxes (2K rounded up to 4 floats)
   int bw, bh; // b/d box
   int fw, fh; // flux box

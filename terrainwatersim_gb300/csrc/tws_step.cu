@@ -11,8 +11,14 @@
 // the flux with a (2K-1)-cell halo into shared memory with TMA
 // (cp.async.bulk.tensor, completion on an mbarrier), recomputes the halo
 // fluxes it needs, and writes d, f and the flow map of its tile once.
-// The halo cells are recomputed redundantly by neighbouring CTAs, so there is
-// no inter-CTA dependency inside a launch.
+// Halo cells are recomputed redundantly by neighbouring CTAs, so there is no
+// inter-CTA dependency inside a launch.
+//
+// STAGES = 2 makes the CTAs persistent: each walks the tiles
+// blockIdx.x, blockIdx.x + gridDim.x, ... and keeps the TMA load of its next
+// tile in flight in a second buffer while it computes the current one, so
+// HBM reads continue through the compute phases.  STAGES = 1 launches one CTA
+// per tile.
 //
 // Arithmetic is IEEE round-to-nearest with no contraction (__fmul_rn etc.),
 // so the result is bit-identical to the FP32 CPU transcription of the shaders.
@@ -22,6 +28,7 @@
 
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <mutex>
 
@@ -44,6 +51,11 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 }
 __device__ __forceinline__ void fence_mbar_init() {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// Orders this thread's view of earlier generic-proxy shared-memory accesses
+// (made visible to it by __syncthreads) before a following TMA write.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
@@ -87,7 +99,7 @@ __device__ bool wait_bounded(uint64_t* bar, uint32_t parity, int* err) {
   const long long t0 = clock64();
   while (!mbar_try_wait(bar, parity)) {
     if (clock64() - t0 > kWaitCycles) {
-      if (threadIdx.x == 0) atomicExch(err, kDevErrWaitTimeout);
+      atomicExch(err, kDevErrWaitTimeout);
       const long long t1 = clock64();
       while (!mbar_try_wait(bar, parity) && clock64() - t1 < kWaitCycles) {
       }
@@ -100,7 +112,7 @@ __device__ bool wait_bounded(uint64_t* bar, uint32_t parity, int* err) {
 // ---- tile geometry -----------------------------------------------------------
 __host__ __device__ constexpr size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
-template <int K, int TX, int TY, bool F16>
+template <int K, int TX, int TY, bool F16, int STAGES>
 struct Tile {
   static constexpr int HX = (2 * K + 3) / 4 * 4;  // x halo of b/d, whole 16-byte units
   static constexpr int HY = 2 * K;                // y halo of b/d
@@ -109,15 +121,20 @@ struct Tile {
   static constexpr int FW = TX + 2 * RF, FH = TY + 2 * RF;
   static constexpr int SW = FW + 2;  // F16 staging width in cells (starts one cell early)
   static constexpr int NB = BW * BH, NF = FW * FH;
-  static constexpr size_t OFF_B = 0;
-  static constexpr size_t OFF_D = align_up(OFF_B + NB * 4, 128);
-  static constexpr size_t OFF_H = align_up(OFF_D + NB * 4, 128);
-  static constexpr size_t OFF_F = align_up(OFF_H + NB * 4, 128);
-  static constexpr size_t OFF_S = align_up(OFF_F + (size_t)NF * 16, 128);
-  static constexpr size_t OFF_BAR = align_up(OFF_S + (F16 ? (size_t)SW * FH * 8 : 0), 128);
-  static constexpr size_t SMEM = OFF_BAR + 16 + 128;  // + slack to align the base
-  static constexpr uint32_t TX_BYTES =
-      (uint32_t)(2 * NB * 4 + (F16 ? SW * FH * 8 : NF * 16));
+  // One stage = what TMA writes for one tile: b, d and the flux box (float4
+  // records for F32 storage, the raw halves for F16 storage).
+  static constexpr size_t ST_B = 0;
+  static constexpr size_t ST_D = align_up((size_t)NB * 4, 128);
+  static constexpr size_t ST_F = align_up(ST_D + (size_t)NB * 4, 128);
+  static constexpr size_t ST_BYTES =
+      align_up(ST_F + (F16 ? (size_t)SW * FH * 8 : (size_t)NF * 16), 128);
+  // Working arrays shared by all stages: surface height h, and for F16 the
+  // float4 copy of the flux.
+  static constexpr size_t OFF_H = STAGES * ST_BYTES;
+  static constexpr size_t OFF_F16 = align_up(OFF_H + (size_t)NB * 4, 128);
+  static constexpr size_t OFF_BAR = align_up(OFF_F16 + (F16 ? (size_t)NF * 16 : 0), 128);
+  static constexpr size_t SMEM = OFF_BAR + 8 * STAGES + 128;  // + slack to align the base
+  static constexpr uint32_t TX_BYTES = (uint32_t)(2 * NB * 4 + (F16 ? SW * FH * 8 : NF * 16));
 };
 
 // F16 storage rounding: the value the next step will read back.
@@ -126,55 +143,30 @@ __device__ __forceinline__ float quantize_f16(float v, float scale, float inv_sc
   return fmul(__half2float(__float2half_rn(s)), inv_scale);
 }
 
-// ---- the kernel --------------------------------------------------------------
-template <int K, int TX, int TY, bool F16>
-__global__ void __launch_bounds__(kThreads)
-    step_kernel(const __grid_constant__ CUtensorMap tm_b, const __grid_constant__ CUtensorMap tm_d,
-                const __grid_constant__ CUtensorMap tm_f, const __grid_constant__ StepArgs a) {
-  using T = Tile<K, TX, TY, F16>;
-  extern __shared__ unsigned char smem_raw[];
-  unsigned char* smem = reinterpret_cast<unsigned char*>(
-      (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~static_cast<uintptr_t>(127));
-  float* sb = reinterpret_cast<float*>(smem + T::OFF_B);
-  float* sd = reinterpret_cast<float*>(smem + T::OFF_D);
-  float* sh = reinterpret_cast<float*>(smem + T::OFF_H);
-  float4* sf = reinterpret_cast<float4*>(smem + T::OFF_F);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + T::OFF_BAR);
+// The three TMA loads of the tile at (x0, y0) into one stage buffer.
+template <class T, bool F16>
+__device__ __forceinline__ void issue_tile(unsigned char* st, uint64_t* bar,
+                                           const CUtensorMap* tm_b, const CUtensorMap* tm_d,
+                                           const CUtensorMap* tm_f, int x0, int y0) {
+  mbar_expect_tx(bar, T::TX_BYTES);
+  tma_load_2d(st + T::ST_B, tm_b, x0 - T::HX, y0 - T::HY, bar);
+  tma_load_2d(st + T::ST_D, tm_d, x0 - T::HX, y0 - T::HY, bar);
+  if (F16) {
+    // cell pairs; x0 - RF - 1 = x0 - 2K is even
+    tma_load_3d(st + T::ST_F, tm_f, 0, (x0 - T::RF - 1) / 2, y0 - T::RF, bar);
+  } else {
+    tma_load_3d(st + T::ST_F, tm_f, 0, x0 - T::RF, y0 - T::RF, bar);
+  }
+}
 
+// K steps of one tile whose loads have landed in (sb, sd, sf-or-staging).
+template <int K, int TX, int TY, bool F16, int STAGES>
+__device__ __forceinline__ void process_tile(const StepArgs& a, int x0, int y0, uint32_t mask,
+                                             float* sb, float* sd, float* sh, float4* sf,
+                                             const unsigned char* staging) {
+  using T = Tile<K, TX, TY, F16, STAGES>;
   const int tid = threadIdx.x;
-  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
   const int W = a.W, H = a.H;
-
-  if (tid == 0) {
-    mbar_init(bar, 1);
-    fence_mbar_init();
-  }
-  __syncthreads();
-  if (tid == 0) {
-    mbar_expect_tx(bar, T::TX_BYTES);
-    tma_load_2d(sb, &tm_b, x0 - T::HX, y0 - T::HY, bar);
-    tma_load_2d(sd, &tm_d, x0 - T::HX, y0 - T::HY, bar);
-    if (F16) {
-      // cell pairs; x0 - RF - 1 = x0 - 2K is even
-      tma_load_3d(smem + T::OFF_S, &tm_f, 0, (x0 - T::RF - 1) / 2, y0 - T::RF, bar);
-    } else {
-      tma_load_3d(sf, &tm_f, 0, x0 - T::RF, y0 - T::RF, bar);
-    }
-  }
-
-  // Which sources can touch this CTA's b/d box.
-  uint32_t mask = 0;
-#pragma unroll
-  for (int k = 0; k < TWS_MAX_SOURCES; ++k) {
-    if (k < a.nsrc) {
-      const DevSource& s = a.src[k];
-      if (s.bx1 >= x0 - T::HX && s.bx0 < x0 + TX + T::HX && s.by1 >= y0 - T::HY &&
-          s.by0 < y0 + TY + T::HY)
-        mask |= 1u << k;
-    }
-  }
-
-  if (!wait_bounded(bar, 0, a.err)) return;
 
   // Phase 0: first step's sources, surface height h = d + b (flowUpdate.comp:34).
   for (int idx = tid; idx < T::NB; idx += kThreads) {
@@ -190,7 +182,7 @@ __global__ void __launch_bounds__(kThreads)
     sh[idx] = fadd(d, sb[idx]);
   }
   if (F16) {
-    const __half2* st = reinterpret_cast<const __half2*>(smem + T::OFF_S);
+    const __half2* st = reinterpret_cast<const __half2*>(staging);
     for (int idx = tid; idx < T::NF; idx += kThreads) {
       const int i = idx / T::FW, j = idx - (idx / T::FW) * T::FW;
       const int s = i * T::SW + j + 1;
@@ -263,10 +255,10 @@ __global__ void __launch_bounds__(kThreads)
         if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
         const int fidx = fi * T::FW + fj;
         const float4 fc = sf[fidx];
-        const float X1 = sf[fidx + 1].y;       // -x outflow of the +x neighbour
-        const float X0 = sf[fidx - 1].x;       // +x outflow of the -x neighbour
-        const float Y1 = sf[fidx + T::FW].w;   // -y outflow of the +y neighbour
-        const float Y0 = sf[fidx - T::FW].z;   // +y outflow of the -y neighbour
+        const float X1 = sf[fidx + 1].y;      // -x outflow of the +x neighbour
+        const float X0 = sf[fidx - 1].x;      // +x outflow of the -x neighbour
+        const float Y1 = sf[fidx + T::FW].w;  // -y outflow of the +y neighbour
+        const float Y0 = sf[fidx - T::FW].z;  // +y outflow of the -y neighbour
         const int bidx = (fi + T::HY - T::RF) * T::BW + (fj + T::HX - T::RF);
         const float in = fadd(fadd(fadd(X1, X0), Y1), Y0);
         const float out = fadd(fadd(fadd(fc.x, fc.y), fc.z), fc.w);
@@ -275,8 +267,10 @@ __global__ void __launch_bounds__(kThreads)
           const size_t g = (size_t)gy * a.pitch + gx;
           a.d_out[g] = dn;
           if (F16) {
-            const __half2 lo = __floats2half2_rn(fmul(fc.x, a.flux_scale), fmul(fc.y, a.flux_scale));
-            const __half2 hi = __floats2half2_rn(fmul(fc.z, a.flux_scale), fmul(fc.w, a.flux_scale));
+            const __half2 lo =
+                __floats2half2_rn(fmul(fc.x, a.flux_scale), fmul(fc.y, a.flux_scale));
+            const __half2 hi =
+                __floats2half2_rn(fmul(fc.z, a.flux_scale), fmul(fc.w, a.flux_scale));
             uint2 packed;
             packed.x = *reinterpret_cast<const uint32_t*>(&lo);
             packed.y = *reinterpret_cast<const uint32_t*>(&hi);
@@ -297,65 +291,136 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// ---- the kernel --------------------------------------------------------------
+template <int K, int TX, int TY, bool F16, int STAGES>
+__global__ void __launch_bounds__(kThreads)
+    step_kernel(const __grid_constant__ CUtensorMap tm_b, const __grid_constant__ CUtensorMap tm_d,
+                const __grid_constant__ CUtensorMap tm_f, const __grid_constant__ StepArgs a) {
+  using T = Tile<K, TX, TY, F16, STAGES>;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~static_cast<uintptr_t>(127));
+  float* sh = reinterpret_cast<float*>(smem + T::OFF_H);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + T::OFF_BAR);
+
+  const int tid = threadIdx.x;
+  const int tiles_x = (a.W + TX - 1) / TX;
+  const int num_tiles = tiles_x * ((a.H + TY - 1) / TY);
+
+  if (tid == 0) {
+#pragma unroll
+    for (int s = 0; s < STAGES; ++s) mbar_init(&bars[s], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (tid == 0) {
+#pragma unroll
+    for (int s = 0; s < STAGES; ++s) {
+      const int t = blockIdx.x + s * gridDim.x;
+      if (t < num_tiles)
+        issue_tile<T, F16>(smem + s * T::ST_BYTES, &bars[s], &tm_b, &tm_d, &tm_f,
+                           (t % tiles_x) * TX, (t / tiles_x) * TY);
+    }
+  }
+
+  int it = 0;
+  for (int t = blockIdx.x; t < num_tiles; t += gridDim.x, ++it) {
+    const int s = STAGES == 1 ? 0 : it % STAGES;
+    const uint32_t parity = (uint32_t)((it / STAGES) & 1);
+    unsigned char* st = smem + s * T::ST_BYTES;
+    float* sb = reinterpret_cast<float*>(st + T::ST_B);
+    float* sd = reinterpret_cast<float*>(st + T::ST_D);
+    float4* sf = F16 ? reinterpret_cast<float4*>(smem + T::OFF_F16)
+                     : reinterpret_cast<float4*>(st + T::ST_F);
+    const int x0 = (t % tiles_x) * TX, y0 = (t / tiles_x) * TY;
+
+    // Which sources can touch this tile's b/d box.
+    uint32_t mask = 0;
+#pragma unroll
+    for (int k = 0; k < TWS_MAX_SOURCES; ++k) {
+      if (k < a.nsrc) {
+        const DevSource& src = a.src[k];
+        if (src.bx1 >= x0 - T::HX && src.bx0 < x0 + TX + T::HX && src.by1 >= y0 - T::HY &&
+            src.by0 < y0 + TY + T::HY)
+          mask |= 1u << k;
+      }
+    }
+
+    const bool ok = wait_bounded(&bars[s], parity, a.err);
+    if (__syncthreads_or(!ok)) return;  // every thread leaves together on a time-out
+
+    process_tile<K, TX, TY, F16, STAGES>(a, x0, y0, mask, sb, sd, sh, sf, st + T::ST_F);
+    __syncthreads();  // stage s, h and the F16 working copy are free again
+
+    if (tid == 0) {
+      const int tn = t + STAGES * gridDim.x;
+      if (tn < num_tiles) {
+        fence_proxy_async_smem();
+        issue_tile<T, F16>(st, &bars[s], &tm_b, &tm_d, &tm_f, (tn % tiles_x) * TX,
+                           (tn / tiles_x) * TY);
+      }
+    }
+  }
+}
+
 // ---- variant table -------------------------------------------------------------
 using KernelFn = void (*)(CUtensorMap, CUtensorMap, CUtensorMap, StepArgs);
 
 struct VariantEntry {
   StepVariant v;
-  const void* fn32;
-  const void* fn16;
+  const void* fn[2];  // [flux storage]
+  size_t smem[2];
+  int ctas_per_sm[2] = {0, 0};  // occupancy, filled on first launch
+  bool attr_set[2] = {false, false};
 };
 
-template <int K, int TX, int TY>
+template <int K, int TX, int TY, int STAGES>
 VariantEntry make_entry() {
-  using T = Tile<K, TX, TY, true>;
-  using T32 = Tile<K, TX, TY, false>;
+  using T32 = Tile<K, TX, TY, false, STAGES>;
+  using T16 = Tile<K, TX, TY, true, STAGES>;
   VariantEntry e;
   e.v.k = K;
   e.v.tx = TX;
   e.v.ty = TY;
+  e.v.stages = STAGES;
   e.v.hx = T32::HX;
   e.v.bw = T32::BW;
   e.v.bh = T32::BH;
   e.v.fw = T32::FW;
   e.v.fh = T32::FH;
-  e.v.smem = T::SMEM;  // the larger of the two
-  e.fn32 = reinterpret_cast<const void*>(&step_kernel<K, TX, TY, false>);
-  e.fn16 = reinterpret_cast<const void*>(&step_kernel<K, TX, TY, true>);
+  e.v.smem = T32::SMEM > T16::SMEM ? T32::SMEM : T16::SMEM;
+  e.fn[TWS_FLUX_F32] = reinterpret_cast<const void*>(&step_kernel<K, TX, TY, false, STAGES>);
+  e.fn[TWS_FLUX_F16] = reinterpret_cast<const void*>(&step_kernel<K, TX, TY, true, STAGES>);
+  e.smem[TWS_FLUX_F32] = T32::SMEM;
+  e.smem[TWS_FLUX_F16] = T16::SMEM;
   return e;
 }
 
-template <int K, int TX, int TY>
-size_t smem_of(bool f16) {
-  return f16 ? Tile<K, TX, TY, true>::SMEM : Tile<K, TX, TY, false>::SMEM;
-}
-
 struct VariantTable {
-  VariantEntry e[16];
-  size_t smem32[16], smem16[16];
+  static constexpr int kMax = 24;
+  VariantEntry e[kMax];
   int n = 0;
-  bool attr_set32[16] = {}, attr_set16[16] = {};
   std::mutex mu;
   VariantTable() {
-    // index: K, tile -- the first entry of each K is its default
-    add<1, 64, 32>();   // 0
-    add<2, 64, 32>();   // 1
-    add<3, 64, 32>();   // 2
-    add<4, 64, 32>();   // 3
-    add<1, 64, 16>();   // 4
-    add<1, 128, 16>();  // 5
-    add<1, 32, 32>();   // 6
-    add<1, 64, 8>();    // 7
-    add<2, 128, 16>();  // 8
-    add<2, 64, 16>();   // 9
-    add<4, 64, 48>();   // 10
+    // Entries 0..3 are the defaults for K = 1..4.
+    add<1, 32, 32, 2>();  // 0  plain, persistent, double-buffered
+    add<2, 64, 16, 2>();  // 1
+    add<3, 64, 32, 2>();  // 2
+    add<4, 64, 32, 2>();  // 3
+    add<1, 64, 16, 2>();  // 4
+    add<1, 64, 32, 2>();  // 5
+    add<1, 32, 16, 2>();  // 6
+    add<1, 32, 32, 1>();  // 7  one CTA per tile
+    add<1, 64, 16, 1>();  // 8
+    add<1, 64, 32, 1>();  // 9
+    add<2, 32, 32, 2>();  // 10
+    add<2, 64, 16, 1>();  // 11
+    add<2, 64, 32, 1>();  // 12
+    add<4, 64, 32, 1>();  // 13
   }
-  template <int K, int TX, int TY>
+  template <int K, int TX, int TY, int STAGES>
   void add() {
-    e[n] = make_entry<K, TX, TY>();
-    smem32[n] = smem_of<K, TX, TY>(false);
-    smem16[n] = smem_of<K, TX, TY>(true);
-    ++n;
+    e[n++] = make_entry<K, TX, TY, STAGES>();
   }
 };
 
@@ -369,12 +434,13 @@ using EncodeTiledFn = PFN_cuTensorMapEncodeTiled_v12000;
 EncodeTiledFn encode_fn(std::string* why) {
   static EncodeTiledFn fn = nullptr;
   static std::once_flag once;
-  static cudaError_t err = cudaSuccess;
   std::call_once(once, [] {
     cudaDriverEntryPointQueryResult q;
     void* p = nullptr;
-    err = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
-    if (err == cudaSuccess && q == cudaDriverEntryPointSuccess) fn = reinterpret_cast<EncodeTiledFn>(p);
+    const cudaError_t err =
+        cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
+    if (err == cudaSuccess && q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
   });
   if (!fn && why) *why = "cuTensorMapEncodeTiled is not available from the driver";
   return fn;
@@ -386,7 +452,7 @@ int step_variant_count() { return table().n; }
 const StepVariant& step_variant(int i) { return table().e[i].v; }
 
 int step_variant_for(int k, int /*flux_storage*/) {
-  // Default tile per temporal depth: the first table entry with that K.
+  // Default tile per temporal depth: entries 0..3 of the table.
   return (k >= 1 && k <= 4) ? k - 1 : -1;
 }
 
@@ -453,22 +519,39 @@ cudaError_t launch_step(int variant, int flux_storage, const CUtensorMap& tm_b,
                         cudaStream_t s) {
   VariantTable& t = table();
   if (variant < 0 || variant >= t.n) return cudaErrorInvalidValue;
-  const bool f16 = flux_storage == TWS_FLUX_F16;
-  const void* fn = f16 ? t.e[variant].fn16 : t.e[variant].fn32;
-  const size_t smem = f16 ? t.smem16[variant] : t.smem32[variant];
+  const int fs = flux_storage == TWS_FLUX_F16 ? TWS_FLUX_F16 : TWS_FLUX_F32;
+  VariantEntry& e = t.e[variant];
+  const void* fn = e.fn[fs];
+  const size_t smem = e.smem[fs];
+  int ctas_per_sm;
   {
     std::lock_guard<std::mutex> lk(t.mu);
-    bool& set = f16 ? t.attr_set16[variant] : t.attr_set32[variant];
-    if (!set) {
-      cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return e;
-      set = true;
+    if (!e.attr_set[fs]) {
+      cudaError_t err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (err != cudaSuccess) return err;
+      int n = 0;
+      err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kThreads, smem);
+      if (err != cudaSuccess) return err;
+      e.ctas_per_sm[fs] = n > 0 ? n : 1;
+      e.attr_set[fs] = true;
     }
+    ctas_per_sm = e.ctas_per_sm[fs];
   }
-  const StepVariant& v = t.e[variant].v;
-  dim3 grid((a.W + v.tx - 1) / v.tx, (a.H + v.ty - 1) / v.ty);
+  const StepVariant& v = e.v;
+  const long long tiles = (long long)((a.W + v.tx - 1) / v.tx) * ((a.H + v.ty - 1) / v.ty);
+  long long blocks = tiles;
+  if (v.stages > 1) {
+    static int sms = 0;
+    if (sms == 0) {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      if (sms <= 0) sms = 1;
+    }
+    blocks = std::min<long long>(tiles, (long long)sms * ctas_per_sm);
+  }
   auto kfn = reinterpret_cast<KernelFn>(const_cast<void*>(fn));
-  kfn<<<grid, kThreads, smem, s>>>(tm_b, tm_d, tm_f, a);
+  kfn<<<(unsigned)blocks, kThreads, smem, s>>>(tm_b, tm_d, tm_f, a);
   count_launch();
   return cudaGetLastError();
 }

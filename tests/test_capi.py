@@ -106,8 +106,9 @@ def test_binding_raises_when_library_missing(tmp_path, monkeypatch):
 def test_variant_table(tws):
     v = tws.variants()
     assert len(v) >= 4
-    assert {k for k, _, _, _ in v} == {1, 2, 3, 4}
-    for k, tx, ty, smem in v:
-        assert tx % 4 == 0 and ty >= 1 and 0 < smem <= 227 * 1024
-    import ctypes as C
-    assert tws.lib().tws_variant_info(len(v), None, None, None, None) == tws.ERR_INVALID
+    assert {k for k, _, _, _, _ in v} == {1, 2, 3, 4}
+    for k, tx, ty, stages, smem in v:
+        assert tx % 4 == 0 and ty >= 1 and stages in (1, 2) and 0 < smem <= 227 * 1024
+    # entries 0..3 are the defaults for K = 1..4
+    assert [v[i][0] for i in range(4)] == [1, 2, 3, 4]
+    assert tws.lib().tws_variant_info(len(v), None, None, None, None, None) == tws.ERR_INVALID

@@ -41,6 +41,7 @@ extern "C" {
 #define TWS_ERR_TIMEOUT -4     /* a device-side bounded wait gave up        */
 #define TWS_ERR_UNSUPPORTED -5 /* option not built into this library        */
 #define TWS_ERR_BUSY -6        /* admission refused (serving loop)          */
+#define TWS_ERR_TOO_LARGE -7   /* input exceeds a fixed-size scratch array  */
 
 /* ---- enums ------------------------------------------------------------ */
 #define TWS_BOUNDARY_CLOSED 0 /* zero flux across the grid border          */
@@ -188,6 +189,34 @@ TWS_API int tws_step(tws_grid* grid, int nsteps);
 /* Total water volume sum(d) * cell_area, accumulated in FP64 on the device
  * (no counterpart in the reference).  Synchronous; deterministic. */
 TWS_API int tws_volume(tws_grid* grid, double* out);
+
+/* Total water volume without allocating anything.  No counterpart in the
+ * reference.
+ *
+ * For callers that must not allocate device memory: a renderer or game loop
+ * that hands out all GPU memory from its own pools, a real-time frame path
+ * that cannot afford the implicit synchronisation cudaMalloc/cudaFree may
+ * cause, or code recording a CUDA graph, where allocation calls are not
+ * allowed.  The caller passes the depth buffer (`pitch` floats per row, e.g.
+ * from tws_get_buffers) and a device pointer `out` for the result; the call
+ * only enqueues two kernels on `stream` (a cudaStream_t, NULL = legacy
+ * default) and returns without waiting.  The sum is FP64, one partial per row
+ * added in row order, times `cell_area`; it equals tws_volume's result to
+ * within FP64 rounding (bit-identical for heights up to 1024 rows).
+ *
+ * Its scratch is one fixed device array of TWS_VOLUME_NOALLOC_MAX_ROWS doubles
+ * (128 KB) inside libtws.so, which every GPU that loads the library holds
+ * until the process exits.  Grids taller than that return
+ * TWS_ERR_TOO_LARGE.  The first call on each device looks up that array's
+ * device address once (cudaGetSymbolAddress); make the first call before any
+ * stream capture.  All calls share the array and it keeps the last call's
+ * partial sums (every partial is rewritten, nothing needs clearing), so two
+ * calls that can run on the GPU at the same time -- on different streams,
+ * or from different host threads -- race and may return wrong sums:
+ * serialise them (one stream, or events). */
+#define TWS_VOLUME_NOALLOC_MAX_ROWS 16384
+TWS_API int tws_volume_noalloc(const float* depth, int width, int height, int pitch,
+                               double cell_area, double* out, void* stream);
 
 /* Copy state to host arrays (each may be NULL).  Flux is returned as 4 floats
  * per cell whatever the storage.  Synchronous. */

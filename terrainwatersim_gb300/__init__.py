@@ -41,6 +41,8 @@ ERR_OOM = -3
 ERR_TIMEOUT = -4
 ERR_UNSUPPORTED = -5
 ERR_BUSY = -6
+ERR_TOO_LARGE = -7
+VOLUME_NOALLOC_MAX_ROWS = 16384
 
 _PKG = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_PKG, "_build", "libtws.so")
@@ -102,6 +104,7 @@ def _declare(L):
         "tws_autotune": ([vp, i, vp], i),
         "tws_step": ([vp, i], i),
         "tws_volume": ([vp, vp], i),
+        "tws_volume_noalloc": ([vp, i, i, i, d, vp, vp], i),
         "tws_download": ([vp, vp, vp, vp], i),
         "tws_download_terrain": ([vp, vp], i),
         "tws_get_buffers": ([vp, vp], i),

@@ -2,6 +2,7 @@
 // volume, the synthetic scene generator and flux format conversion.
 
 #include <algorithm>
+#include <mutex>
 
 #include "tws_device.cuh"
 #include "tws_internal.h"
@@ -319,4 +320,55 @@ extern "C" TWS_API int tws_scene_rain_disks(uint64_t seed, int W, int H, int rad
     out[k].rate = rate;
   }
   return TWS_OK;
+}
+
+// ---- total volume without allocation ------------------------------------------
+// Scratch of tws_volume_noalloc: one FP64 partial sum per grid row, in a fixed
+// array that lives in the module image, so the call needs no cudaMalloc.
+// Every GPU that loads this library holds it (128 KB) until the process
+// exits.  Host code must not pass `g_volume_row_sums` itself to a kernel: on
+// the host that name is only a stand-in for the symbol, not a device address;
+// the device address is looked up once per device below.
+static __device__ __align__(256) double g_volume_row_sums[TWS_VOLUME_NOALLOC_MAX_ROWS];
+
+namespace {
+
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+double* g_noalloc_scratch[kNoallocMaxDevices] = {};
+
+// Device address of the scratch on the current device; looked up on the first
+// call per device (cudaGetSymbolAddress, with that device current).
+cudaError_t noalloc_scratch(double** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kNoallocMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_scratch[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_volume_row_sums);
+    if (e != cudaSuccess) return e;
+    g_noalloc_scratch[dev] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_scratch[dev];
+  return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" TWS_API int tws_volume_noalloc(const float* depth, int width, int height, int pitch,
+                                          double cell_area, double* out, void* stream) {
+  if (!depth || !out || width < 1 || height < 1 || pitch < width) return TWS_ERR_INVALID;
+  if (height > TWS_VOLUME_NOALLOC_MAX_ROWS) return TWS_ERR_TOO_LARGE;
+  double* scratch = nullptr;
+  if (noalloc_scratch(&scratch) != cudaSuccess) return TWS_ERR_CUDA;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // One block per row: block r writes partial r (every partial is rewritten,
+  // so nothing needs clearing); one block then adds the partials in row order.
+  tws::volume_rows_kernel<<<height, tws::kVolThreads, 0, st>>>(depth, width, height, pitch,
+                                                               scratch);
+  tws::volume_final_kernel<<<1, tws::kVolThreads, 0, st>>>(scratch, height, cell_area, out);
+  tws::count_launch(2);
+  return cudaGetLastError() == cudaSuccess ? TWS_OK : TWS_ERR_CUDA;
 }

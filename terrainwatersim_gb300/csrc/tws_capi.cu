@@ -192,6 +192,9 @@ TWS_API const char* tws_error_string(int code) {
     case TWS_ERR_TIMEOUT: return "device-side wait timed out";
     case TWS_ERR_UNSUPPORTED: return "unsupported option";
     case TWS_ERR_BUSY: return "admission refused";
+    case TWS_ERR_TOO_LARGE:
+      return "grid too large for the fixed scratch of tws_volume_noalloc "
+             "(more than TWS_VOLUME_NOALLOC_MAX_ROWS rows)";
     default: return "unknown error";
   }
 }

@@ -161,13 +161,17 @@ int enqueue_steps(tws_grid* g, int nsteps) {
     const int k = std::min(kmax, left);
     // the remainder of a chain that is not a multiple of K runs shallower
     const int variant = k == kmax ? main_variant : step_variant_for(k, g->flux_storage);
-    VariantMaps* m = maps_for(g, variant, &why);
-    if (!m) return fail(g, TWS_ERR_CUDA, why);
+    VariantMaps* m = nullptr;
+    if (step_variant(variant).kind == kKindTile) {
+      m = maps_for(g, variant, &why);
+      if (!m) return fail(g, TWS_ERR_CUDA, why);
+    }
     const int nxt = g->cur ^ 1;
     a.d_out = g->d[nxt];
     a.f_out = g->f[nxt];
-    cudaError_t e = launch_step(variant, g->flux_storage, m->b, m->d[g->cur], m->f[g->cur], a,
-                                g->stream);
+    cudaError_t e = launch_step(variant, g->flux_storage, m ? &m->b : nullptr,
+                                m ? &m->d[g->cur] : nullptr, m ? &m->f[g->cur] : nullptr, g->b,
+                                g->d[g->cur], g->f[g->cur], a, g->stream);
     if (e != cudaSuccess) return cuda_fail(g, e, "step kernel launch");
     g->cur = nxt;
     left -= k;

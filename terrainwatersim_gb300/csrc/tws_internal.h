@@ -41,11 +41,15 @@ struct StepVariant {
   int k;      // steps per launch
   int tx, ty; // interior tile
   int stages; // 1: one CTA per tile; 2: persistent CTAs, next tile prefetched
+  int kind;   // kKindTile (TMA-staged tiles) or kKindStream (register streaming, K = 1)
+  int ry;     // kKindStream: rows per warp strip
   int hx;     // x halo of the b/d boxes (2K rounded up to 4 floats)
   int bw, bh; // b/d box
   int fw, fh; // flux box
   size_t smem;
 };
+
+enum : int { kKindTile = 0, kKindStream = 1 };
 
 // Device error codes written to StepArgs::err.
 enum : int { kDevErrNone = 0, kDevErrWaitTimeout = 1 };
@@ -54,9 +58,14 @@ enum : int { kDevErrNone = 0, kDevErrWaitTimeout = 1 };
 int step_variant_count();
 const StepVariant& step_variant(int i);
 int step_variant_for(int k, int flux_storage);
-cudaError_t launch_step(int variant, int flux_storage, const CUtensorMap& tm_b,
-                        const CUtensorMap& tm_d, const CUtensorMap& tm_f, const StepArgs& a,
-                        cudaStream_t s);
+// Tile variants read through the tensor maps, stream variants through the
+// raw pointers (b, d, f of the current state).
+cudaError_t launch_step(int variant, int flux_storage, const CUtensorMap* tm_b,
+                        const CUtensorMap* tm_d, const CUtensorMap* tm_f, const float* b,
+                        const float* d, const void* f, const StepArgs& a, cudaStream_t s);
+// tws_stream.cu
+cudaError_t launch_stream_step(int ry, int flux_storage, const float* b, const float* d,
+                               const void* f, const StepArgs& a, cudaStream_t s);
 cudaError_t encode_step_maps(int variant, int flux_storage, int W, int H, int pitch,
                              const float* b, const float* d, const void* f, CUtensorMap* tm_b,
                              CUtensorMap* tm_d, CUtensorMap* tm_f, std::string* why);

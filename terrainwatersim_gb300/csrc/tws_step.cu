@@ -386,6 +386,8 @@ VariantEntry make_entry() {
   e.v.tx = TX;
   e.v.ty = TY;
   e.v.stages = STAGES;
+  e.v.kind = kKindTile;
+  e.v.ry = 0;
   e.v.hx = T32::HX;
   e.v.bw = T32::BW;
   e.v.bh = T32::BH;
@@ -421,10 +423,24 @@ struct VariantTable {
     add<2, 32, 32, 1>();  // 10
     add<2, 64, 16, 2>();  // 11
     add<2, 64, 32, 1>();  // 12
+    add_stream(64);       // 13 register streaming, 30-column strips x 64 rows
+    add_stream(32);       // 14
+    add_stream(128);      // 15
   }
   template <int K, int TX, int TY, int STAGES>
   void add() {
     e[n++] = make_entry<K, TX, TY, STAGES>();
+  }
+  void add_stream(int ry) {
+    VariantEntry s{};
+    s.v.k = 1;
+    s.v.tx = 30;
+    s.v.ty = ry;
+    s.v.stages = 1;
+    s.v.kind = kKindStream;
+    s.v.ry = ry;
+    s.v.smem = 0;
+    e[n++] = s;
   }
 };
 
@@ -518,13 +534,15 @@ cudaError_t encode_step_maps(int variant, int flux_storage, int W, int H, int pi
   return cudaSuccess;
 }
 
-cudaError_t launch_step(int variant, int flux_storage, const CUtensorMap& tm_b,
-                        const CUtensorMap& tm_d, const CUtensorMap& tm_f, const StepArgs& a,
-                        cudaStream_t s) {
+cudaError_t launch_step(int variant, int flux_storage, const CUtensorMap* tm_b,
+                        const CUtensorMap* tm_d, const CUtensorMap* tm_f, const float* b,
+                        const float* d, const void* f, const StepArgs& a, cudaStream_t s) {
   VariantTable& t = table();
   if (variant < 0 || variant >= t.n) return cudaErrorInvalidValue;
   const int fs = flux_storage == TWS_FLUX_F16 ? TWS_FLUX_F16 : TWS_FLUX_F32;
   VariantEntry& e = t.e[variant];
+  if (e.v.kind == kKindStream) return launch_stream_step(e.v.ry, fs, b, d, f, a, s);
+  if (!tm_b || !tm_d || !tm_f) return cudaErrorInvalidValue;
   const void* fn = e.fn[fs];
   const size_t smem = e.smem[fs];
   int ctas_per_sm;
@@ -555,7 +573,7 @@ cudaError_t launch_step(int variant, int flux_storage, const CUtensorMap& tm_b,
     blocks = std::min<long long>(tiles, (long long)sms * ctas_per_sm);
   }
   auto kfn = reinterpret_cast<KernelFn>(const_cast<void*>(fn));
-  kfn<<<(unsigned)blocks, kThreads, smem, s>>>(tm_b, tm_d, tm_f, a);
+  kfn<<<(unsigned)blocks, kThreads, smem, s>>>(*tm_b, *tm_d, *tm_f, a);
   count_launch();
   return cudaGetLastError();
 }

@@ -228,6 +228,43 @@ TWS_API int tws_download_terrain(tws_grid* grid, float* terrain);
  * Terrain.cpp:288, 323-330). */
 TWS_API int tws_get_buffers(tws_grid* grid, tws_buffers* out);
 
+/* ---- batches -----------------------------------------------------------
+ * Many grids of different sizes advanced together: one persistent launch per
+ * step covers the tiles of every member grid, and chains of 16 steps are
+ * replayed from CUDA graphs.  Member grids keep their own buffers,
+ * parameters and sources; while in a batch their work is ordered on the
+ * batch's stream.  Grids can join and leave between calls (continuous
+ * batching); each call advances every member by its own step count.  No
+ * counterpart in the reference, which simulates one grid. */
+typedef struct tws_batch tws_batch;
+
+TWS_API int tws_batch_create(int flux_storage, void* stream, tws_batch** out);
+TWS_API int tws_batch_destroy(tws_batch* batch); /* removes the members first */
+/* The grid's queued work completes first; it must have the batch's flux storage. */
+TWS_API int tws_batch_add(tws_batch* batch, tws_grid* grid);
+TWS_API int tws_batch_remove(tws_batch* batch, tws_grid* grid);
+TWS_API int tws_batch_size(tws_batch* batch);
+/* Batched kernel variants: K steps per launch and the tile. */
+TWS_API int tws_batch_variant_count(void);
+TWS_API int tws_batch_variant_info(int variant, int* steps_per_launch, int* tile_x, int* tile_y);
+TWS_API int tws_batch_set_variant(tws_batch* batch, int variant);
+/* Times every batched variant on the members' current state (restored
+ * afterwards) and keeps the fastest.  Synchronous. */
+TWS_API int tws_batch_autotune(tws_batch* batch, int trial_steps, int* chosen);
+/* 1 (default): replay chains from CUDA graphs; 0: launch each step directly. */
+TWS_API int tws_batch_use_graphs(tws_batch* batch, int enable);
+/* Every member advances `nsteps` steps.  Asynchronous. */
+TWS_API int tws_batch_step(tws_batch* batch, int nsteps);
+/* Member i (in the order added, removals closing the gaps) advances
+ * nsteps[i] steps; n must equal tws_batch_size.  Asynchronous. */
+TWS_API int tws_batch_step_each(tws_batch* batch, const int* nsteps, int n);
+/* Waits for the batch and reports any member's device-side error. */
+TWS_API int tws_batch_sync(tws_batch* batch);
+TWS_API void* tws_batch_stream(tws_batch* batch);
+TWS_API const char* tws_batch_last_error(tws_batch* batch);
+/* Chains run and chains replayed from a graph so far. */
+TWS_API int tws_batch_stats(tws_batch* batch, uint64_t* chains, uint64_t* graph_launches);
+
 /* Block the host until the grid's queued work is done; reports a device-side
  * error (TWS_ERR_TIMEOUT) raised by any kernel of this grid. */
 TWS_API int tws_sync(tws_grid* grid);

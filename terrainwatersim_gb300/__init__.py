@@ -113,6 +113,22 @@ def _declare(L):
         "tws_error_string": ([i], C.c_char_p),
         "tws_last_error": ([vp], C.c_char_p),
         "tws_launch_count": ([], u64),
+        "tws_batch_create": ([i, vp, vp], i),
+        "tws_batch_destroy": ([vp], i),
+        "tws_batch_add": ([vp, vp], i),
+        "tws_batch_remove": ([vp, vp], i),
+        "tws_batch_size": ([vp], i),
+        "tws_batch_variant_count": ([], i),
+        "tws_batch_variant_info": ([i, vp, vp, vp], i),
+        "tws_batch_set_variant": ([vp, i], i),
+        "tws_batch_autotune": ([vp, i, vp], i),
+        "tws_batch_use_graphs": ([vp, i], i),
+        "tws_batch_step": ([vp, i], i),
+        "tws_batch_step_each": ([vp, vp, i], i),
+        "tws_batch_sync": ([vp], i),
+        "tws_batch_stream": ([vp], vp),
+        "tws_batch_last_error": ([vp], C.c_char_p),
+        "tws_batch_stats": ([vp, vp, vp], i),
         "tws_version": ([], C.c_char_p),
     }
     for name, (args, res) in sig.items():
@@ -304,3 +320,91 @@ class Grid:
         out = Buffers()
         _check(lib().tws_get_buffers(self._h, C.byref(out)), self._h)
         return out
+
+
+def batch_variants():
+    """[(steps_per_launch, tile_x, tile_y)] of the batched kernel."""
+    L = lib()
+    out = []
+    for i in range(L.tws_batch_variant_count()):
+        k, tx, ty = C.c_int(), C.c_int(), C.c_int()
+        _check(L.tws_batch_variant_info(i, C.byref(k), C.byref(tx), C.byref(ty)))
+        out.append((k.value, tx.value, ty.value))
+    return out
+
+
+class Batch:
+    """Many grids advanced together by one persistent launch per step, chains
+    of 16 steps replayed from CUDA graphs (tws_batch_* in include/tws.h)."""
+
+    def __init__(self, flux_storage: int = FLUX_F32, stream: int | None = None):
+        h = C.c_void_p()
+        _check(lib().tws_batch_create(flux_storage, C.c_void_p(stream) if stream else None,
+                                      C.byref(h)))
+        self._h = h
+        self.grids = []
+
+    def _check(self, code):
+        if code != TWS_OK:
+            L = lib()
+            raise TwsError(code, f"{L.tws_error_string(code).decode()}: "
+                                 f"{L.tws_batch_last_error(self._h).decode()}")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().tws_batch_destroy(self._h)
+            self._h = None
+            self.grids = []
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return lib().tws_batch_stream(self._h) or 0
+
+    def add(self, grid: Grid):
+        self._check(lib().tws_batch_add(self._h, grid.handle))
+        self.grids.append(grid)
+
+    def remove(self, grid: Grid):
+        self._check(lib().tws_batch_remove(self._h, grid.handle))
+        self.grids.remove(grid)
+
+    def __len__(self):
+        return lib().tws_batch_size(self._h)
+
+    def set_variant(self, variant: int):
+        self._check(lib().tws_batch_set_variant(self._h, variant))
+
+    def use_graphs(self, enable: bool):
+        self._check(lib().tws_batch_use_graphs(self._h, 1 if enable else 0))
+
+    def autotune(self, trial_steps: int = 32) -> int:
+        out = C.c_int()
+        self._check(lib().tws_batch_autotune(self._h, trial_steps, C.byref(out)))
+        return out.value
+
+    def step(self, nsteps: int):
+        self._check(lib().tws_batch_step(self._h, nsteps))
+
+    def step_each(self, nsteps):
+        arr = (C.c_int * max(1, len(nsteps)))(*[int(n) for n in nsteps])
+        self._check(lib().tws_batch_step_each(self._h, arr, len(nsteps)))
+
+    def sync(self):
+        self._check(lib().tws_batch_sync(self._h))
+
+    def stats(self):
+        a, b = C.c_uint64(), C.c_uint64()
+        self._check(lib().tws_batch_stats(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value

@@ -53,6 +53,8 @@ struct tws_grid {
   double* vol_host = nullptr;  // pinned
   int* err = nullptr;          // device error word
   int* err_host = nullptr;     // pinned
+  tws_batch* batch = nullptr;  // batch this grid belongs to (its stream is the batch's)
+  cudaStream_t home_stream = nullptr;
   std::string last_error;
 };
 
@@ -136,6 +138,24 @@ int chosen_variant(const tws_grid* g) {
   }
   const int k = g->steps_per_launch > 0 ? g->steps_per_launch : default_steps_per_launch(g);
   return step_variant_for(k, g->flux_storage);
+}
+
+StepArgs make_step_args(const tws_grid* g) {
+  StepArgs a{};
+  a.W = g->W;
+  a.H = g->H;
+  a.pitch = g->pitch;
+  a.kf = g->params.flow_friction_per_step;
+  a.ka = g->params.water_acceleration_per_step;
+  a.c = g->params.cell_area_inv_time_scaled;
+  a.closed = g->params.boundary == TWS_BOUNDARY_CLOSED;
+  a.nsrc = g->nsrc;
+  for (int i = 0; i < g->nsrc; ++i) a.src[i] = make_dev_source(g->src[i]);
+  a.v_out = g->v;
+  a.flux_scale = g->flux_scale;
+  a.flux_inv_scale = 1.0f / g->flux_scale;
+  a.err = g->err;
+  return a;
 }
 
 int enqueue_steps(tws_grid* g, int nsteps) {
@@ -306,6 +326,7 @@ TWS_API int tws_create(int width, int height, const tws_sim_params* params, int 
 
 TWS_API int tws_destroy(tws_grid* g) {
   if (!g) return TWS_ERR_INVALID;
+  if (g->batch) tws_batch_remove(g->batch, g);
   if (g->stream) cudaStreamSynchronize(g->stream);
   cudaFree(g->b);
   cudaFree(g->d[0]);
@@ -584,6 +605,438 @@ TWS_API int tws_sync(tws_grid* g) {
   TWS_CUDA(g, cudaStreamSynchronize(g->stream), "sync");
   if (*g->err_host != kDevErrNone)
     return fail(g, TWS_ERR_TIMEOUT, "a kernel gave up waiting for its tile loads");
+  return TWS_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Batches: many grids advanced by one persistent launch per step.
+//
+// A chain is up to kChainSteps steps.  Before a chain the host writes the
+// table of participating grids (their tensor maps, step arguments, buffers,
+// ping-pong parity and the number of launches each takes) and the prefix of
+// their tile counts into device memory with one stream-ordered copy, then
+// replays a CUDA graph of the chain's launches.  The launches read everything
+// from that table, so one graph per (variant, chain length) serves every
+// composition of the batch: grids join and leave between chains (continuous
+// batching) without re-capture.
+// ===========================================================================
+
+namespace {
+constexpr int kChainSteps = 16;
+}
+
+struct tws_batch {
+  int flux_storage = TWS_FLUX_F32;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::vector<tws_grid*> grids;
+  int variant = 0;  // batched kernel variant
+  bool use_graphs = true;
+  int cap = 0;  // table capacity (grids)
+  BatchGrid* d_grids = nullptr;
+  int* d_base = nullptr;
+  int* d_hdr = nullptr;
+  // host staging, two slots so that filling one does not wait for the copy of the other
+  BatchGrid* h_grids[2] = {nullptr, nullptr};
+  int* h_base[2] = {nullptr, nullptr};
+  int* h_hdr[2] = {nullptr, nullptr};
+  cudaEvent_t copied[2] = {nullptr, nullptr};
+  int slot = 0;
+  struct Graph {
+    int variant, launches;
+    cudaGraphExec_t exec;
+  };
+  std::vector<Graph> graphs;
+  uint64_t chains = 0, graph_launches = 0;
+  std::string last_error;
+};
+
+namespace {
+
+int bfail(tws_batch* b, int code, const std::string& msg) {
+  if (b) b->last_error = msg;
+  return code;
+}
+
+void drop_graphs(tws_batch* b) {
+  for (auto& gr : b->graphs) cudaGraphExecDestroy(gr.exec);
+  b->graphs.clear();
+}
+
+void free_table(tws_batch* b) {
+  cudaFree(b->d_grids);
+  cudaFree(b->d_base);
+  cudaFree(b->d_hdr);
+  for (int s = 0; s < 2; ++s) {
+    if (b->h_grids[s]) cudaFreeHost(b->h_grids[s]);
+    if (b->h_base[s]) cudaFreeHost(b->h_base[s]);
+    if (b->h_hdr[s]) cudaFreeHost(b->h_hdr[s]);
+    b->h_grids[s] = nullptr;
+    b->h_base[s] = nullptr;
+    b->h_hdr[s] = nullptr;
+  }
+  b->d_grids = nullptr;
+  b->d_base = nullptr;
+  b->d_hdr = nullptr;
+  b->cap = 0;
+}
+
+// Grow the table to hold n grids (graphs reference the device arrays, so they
+// are dropped when the arrays move).
+int ensure_capacity(tws_batch* b, int n) {
+  if (n <= b->cap) return TWS_OK;
+  cudaStreamSynchronize(b->stream);
+  drop_graphs(b);
+  free_table(b);
+  int cap = 16;
+  while (cap < n) cap *= 2;
+  if (cudaMalloc(&b->d_grids, sizeof(BatchGrid) * cap) != cudaSuccess ||
+      cudaMalloc(&b->d_base, sizeof(int) * (cap + 1)) != cudaSuccess ||
+      cudaMalloc(&b->d_hdr, sizeof(int) * 4) != cudaSuccess) {
+    cudaGetLastError();
+    free_table(b);
+    return bfail(b, TWS_ERR_OOM, "batch table allocation failed");
+  }
+  for (int s = 0; s < 2; ++s) {
+    if (cudaMallocHost(&b->h_grids[s], sizeof(BatchGrid) * cap) != cudaSuccess ||
+        cudaMallocHost(&b->h_base[s], sizeof(int) * (cap + 1)) != cudaSuccess ||
+        cudaMallocHost(&b->h_hdr[s], sizeof(int) * 4) != cudaSuccess) {
+      cudaGetLastError();
+      free_table(b);
+      return bfail(b, TWS_ERR_OOM, "batch staging allocation failed");
+    }
+  }
+  b->cap = cap;
+  return TWS_OK;
+}
+
+int run_launches(tws_batch* b, int variant, int launches) {
+  for (int i = 0; i < launches; ++i) {
+    cudaError_t e = launch_batch_step(variant, b->flux_storage, b->d_grids, b->d_base, b->d_hdr, i,
+                                      b->stream);
+    if (e != cudaSuccess) return bfail(b, TWS_ERR_CUDA, std::string("batch launch: ") + cudaGetErrorString(e));
+  }
+  return TWS_OK;
+}
+
+cudaGraphExec_t graph_for(tws_batch* b, int variant, int launches) {
+  for (auto& gr : b->graphs)
+    if (gr.variant == variant && gr.launches == launches) return gr.exec;
+  if (prepare_batch_variant(variant, b->flux_storage) != cudaSuccess) return nullptr;
+  cudaGraph_t graph = nullptr;
+  if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    return nullptr;
+  const int rc = run_launches(b, variant, launches);
+  const cudaError_t ee = cudaStreamEndCapture(b->stream, &graph);
+  if (rc != TWS_OK || ee != cudaSuccess || !graph) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    return nullptr;
+  }
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ie != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  b->graphs.push_back({variant, launches, exec});
+  return exec;
+}
+
+// One chain: grid i takes launches[i] launches of `variant` (K steps each).
+int run_chain(tws_batch* b, int variant, const std::vector<int>& launches) {
+  int k, tx, ty, sv;
+  batch_variant_info(variant, &k, &tx, &ty, &sv);
+  const int n = (int)b->grids.size();
+  int rc = ensure_capacity(b, n);
+  if (rc != TWS_OK) return rc;
+  // wait until the copy that last read this staging slot has completed
+  const int s = b->slot;
+  b->slot ^= 1;
+  if (b->copied[s]) cudaEventSynchronize(b->copied[s]);
+  BatchGrid* hg = b->h_grids[s];
+  int* hb = b->h_base[s];
+  int m = 0, units = 0, max_l = 0;
+  std::string why;
+  for (int i = 0; i < n; ++i) {
+    if (launches[i] <= 0) continue;
+    tws_grid* g = b->grids[i];
+    VariantMaps* maps = maps_for(g, sv, &why);
+    if (!maps) return bfail(b, TWS_ERR_CUDA, why);
+    BatchGrid& e = hg[m];
+    e.tm_b = maps->b;
+    e.tm_d[0] = maps->d[0];
+    e.tm_d[1] = maps->d[1];
+    e.tm_f[0] = maps->f[0];
+    e.tm_f[1] = maps->f[1];
+    e.a = make_step_args(g);
+    e.d[0] = g->d[0];
+    e.d[1] = g->d[1];
+    e.f[0] = g->f[0];
+    e.f[1] = g->f[1];
+    e.v = g->v;
+    e.cur = g->cur;
+    e.launches = launches[i];
+    e.tiles_x = (g->W + tx - 1) / tx;
+    hb[m] = units;
+    units += e.tiles_x * ((g->H + ty - 1) / ty);
+    max_l = std::max(max_l, launches[i]);
+    ++m;
+  }
+  if (m == 0) return TWS_OK;
+  hb[m] = units;
+  b->h_hdr[s][0] = m;
+  cudaMemcpyAsync(b->d_grids, hg, sizeof(BatchGrid) * m, cudaMemcpyHostToDevice, b->stream);
+  cudaMemcpyAsync(b->d_base, hb, sizeof(int) * (m + 1), cudaMemcpyHostToDevice, b->stream);
+  cudaMemcpyAsync(b->d_hdr, b->h_hdr[s], sizeof(int) * 4, cudaMemcpyHostToDevice, b->stream);
+  if (!b->copied[s]) cudaEventCreateWithFlags(&b->copied[s], cudaEventDisableTiming);
+  cudaEventRecord(b->copied[s], b->stream);
+  cudaGraphExec_t exec = b->use_graphs ? graph_for(b, variant, max_l) : nullptr;
+  if (exec) {
+    if (cudaGraphLaunch(exec, b->stream) != cudaSuccess)
+      return bfail(b, TWS_ERR_CUDA, "graph launch failed");
+    count_launch((uint64_t)max_l);
+    ++b->graph_launches;
+  } else {
+    rc = run_launches(b, variant, max_l);
+    if (rc != TWS_OK) return rc;
+  }
+  ++b->chains;
+  // each launch flips a grid's ping-pong buffer once
+  for (int i = 0; i < n; ++i)
+    if (launches[i] > 0) b->grids[i]->cur ^= (launches[i] & 1);
+  return TWS_OK;
+}
+
+// Advance member i by steps[i] steps (chains of up to kChainSteps).
+int batch_advance(tws_batch* b, std::vector<int> left) {
+  int k;
+  batch_variant_info(b->variant, &k, nullptr, nullptr, nullptr);
+  const int n = (int)b->grids.size();
+  const int per_chain = std::max(1, kChainSteps / k);  // launches per chain
+  std::vector<int> launches(n);
+  for (;;) {
+    bool work = false;
+    for (int i = 0; i < n; ++i) {
+      launches[i] = std::min(left[i] / k, per_chain);
+      work |= launches[i] > 0;
+    }
+    if (!work) break;
+    const int rc = run_chain(b, b->variant, launches);
+    if (rc != TWS_OK) return rc;
+    for (int i = 0; i < n; ++i) left[i] -= launches[i] * k;
+  }
+  // steps left over when K does not divide a grid's count: one-step launches
+  bool any = false;
+  for (int i = 0; i < n; ++i) any |= left[i] > 0;
+  if (any) {
+    int k1 = -1;
+    for (int v = 0; v < batch_variant_count(); ++v) {
+      int kv;
+      batch_variant_info(v, &kv, nullptr, nullptr, nullptr);
+      if (kv == 1) {
+        k1 = v;
+        break;
+      }
+    }
+    if (k1 < 0) return bfail(b, TWS_ERR_UNSUPPORTED, "no one-step batched variant");
+    return run_chain(b, k1, left);
+  }
+  return TWS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+TWS_API int tws_batch_create(int flux_storage, void* stream, tws_batch** out) {
+  if (!out || (flux_storage != TWS_FLUX_F32 && flux_storage != TWS_FLUX_F16)) return TWS_ERR_INVALID;
+  *out = nullptr;
+  tws_batch* b = new (std::nothrow) tws_batch();
+  if (!b) return TWS_ERR_OOM;
+  b->flux_storage = flux_storage;
+  if (stream) {
+    b->stream = static_cast<cudaStream_t>(stream);
+  } else {
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete b;
+      return TWS_ERR_CUDA;
+    }
+    b->own_stream = true;
+  }
+  *out = b;
+  return TWS_OK;
+}
+
+TWS_API int tws_batch_remove(tws_batch* b, tws_grid* g) {
+  if (!b || !g || g->batch != b) return bfail(b, TWS_ERR_INVALID, "grid is not in this batch");
+  cudaStreamSynchronize(b->stream);
+  b->grids.erase(std::find(b->grids.begin(), b->grids.end(), g));
+  g->stream = g->home_stream;
+  g->batch = nullptr;
+  return TWS_OK;
+}
+
+TWS_API int tws_batch_destroy(tws_batch* b) {
+  if (!b) return TWS_ERR_INVALID;
+  while (!b->grids.empty()) tws_batch_remove(b, b->grids.back());
+  cudaStreamSynchronize(b->stream);
+  drop_graphs(b);
+  free_table(b);
+  for (int s = 0; s < 2; ++s)
+    if (b->copied[s]) cudaEventDestroy(b->copied[s]);
+  if (b->own_stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return TWS_OK;
+}
+
+TWS_API int tws_batch_add(tws_batch* b, tws_grid* g) {
+  if (!b || !g) return TWS_ERR_INVALID;
+  if (g->batch) return bfail(b, TWS_ERR_INVALID, "grid already belongs to a batch");
+  if (g->flux_storage != b->flux_storage)
+    return bfail(b, TWS_ERR_INVALID, "grid flux storage differs from the batch's");
+  // the grid's queued work finishes first; from now on it is ordered on the batch stream
+  if (cudaStreamSynchronize(g->stream) != cudaSuccess)
+    return bfail(b, TWS_ERR_CUDA, "grid stream failed");
+  g->home_stream = g->stream;
+  g->stream = b->stream;
+  g->batch = b;
+  b->grids.push_back(g);
+  return TWS_OK;
+}
+
+TWS_API int tws_batch_size(tws_batch* b) { return b ? (int)b->grids.size() : 0; }
+
+TWS_API int tws_batch_variant_count(void) { return batch_variant_count(); }
+
+TWS_API int tws_batch_variant_info(int i, int* k, int* tx, int* ty) {
+  if (i < 0 || i >= batch_variant_count()) return TWS_ERR_INVALID;
+  batch_variant_info(i, k, tx, ty, nullptr);
+  return TWS_OK;
+}
+
+TWS_API int tws_batch_set_variant(tws_batch* b, int variant) {
+  if (!b || variant < 0 || variant >= batch_variant_count())
+    return bfail(b, TWS_ERR_INVALID, "no such batched variant");
+  b->variant = variant;
+  return TWS_OK;
+}
+
+TWS_API int tws_batch_use_graphs(tws_batch* b, int enable) {
+  if (!b) return TWS_ERR_INVALID;
+  b->use_graphs = enable != 0;
+  return TWS_OK;
+}
+
+TWS_API int tws_batch_step(tws_batch* b, int nsteps) {
+  if (!b || nsteps < 0) return bfail(b, TWS_ERR_INVALID, "bad step count");
+  return batch_advance(b, std::vector<int>(b->grids.size(), nsteps));
+}
+
+TWS_API int tws_batch_step_each(tws_batch* b, const int* nsteps, int n) {
+  if (!b || !nsteps || n != (int)b->grids.size()) return bfail(b, TWS_ERR_INVALID, "bad step list");
+  for (int i = 0; i < n; ++i)
+    if (nsteps[i] < 0) return bfail(b, TWS_ERR_INVALID, "negative step count");
+  return batch_advance(b, std::vector<int>(nsteps, nsteps + n));
+}
+
+TWS_API int tws_batch_autotune(tws_batch* b, int trial_steps, int* chosen) {
+  if (!b || trial_steps < 1) return bfail(b, TWS_ERR_INVALID, "trial_steps must be positive");
+  const int n = (int)b->grids.size();
+  if (n == 0) return bfail(b, TWS_ERR_INVALID, "empty batch");
+  cudaStreamSynchronize(b->stream);
+  // save every member's state; the trials run on it and it is restored after
+  struct Saved {
+    float* d;
+    void* f;
+    float2* v;
+    int cur;
+  };
+  std::vector<Saved> saved(n);
+  for (int i = 0; i < n; ++i) {
+    tws_grid* g = b->grids[i];
+    const size_t cells = (size_t)g->pitch * g->H, fb = flux_bytes_per_cell(g->flux_storage);
+    saved[i].cur = g->cur;
+    if (cudaMallocAsync(&saved[i].d, cells * 4, b->stream) != cudaSuccess ||
+        cudaMallocAsync(&saved[i].f, cells * fb, b->stream) != cudaSuccess ||
+        cudaMallocAsync(&saved[i].v, cells * 8, b->stream) != cudaSuccess)
+      return bfail(b, TWS_ERR_OOM, "autotune state copy");
+    cudaMemcpyAsync(saved[i].d, g->d[g->cur], cells * 4, cudaMemcpyDeviceToDevice, b->stream);
+    cudaMemcpyAsync(saved[i].f, g->f[g->cur], cells * fb, cudaMemcpyDeviceToDevice, b->stream);
+    cudaMemcpyAsync(saved[i].v, g->v, cells * 8, cudaMemcpyDeviceToDevice, b->stream);
+  }
+  auto restore = [&]() {
+    for (int i = 0; i < n; ++i) {
+      tws_grid* g = b->grids[i];
+      const size_t cells = (size_t)g->pitch * g->H, fb = flux_bytes_per_cell(g->flux_storage);
+      g->cur = saved[i].cur;
+      cudaMemcpyAsync(g->d[g->cur], saved[i].d, cells * 4, cudaMemcpyDeviceToDevice, b->stream);
+      cudaMemcpyAsync(g->f[g->cur], saved[i].f, cells * fb, cudaMemcpyDeviceToDevice, b->stream);
+      cudaMemcpyAsync(g->v, saved[i].v, cells * 8, cudaMemcpyDeviceToDevice, b->stream);
+    }
+  };
+  const int steps = (trial_steps + 2 * kChainSteps - 1) / (2 * kChainSteps) * (2 * kChainSteps);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int saved_variant = b->variant;
+  float best_ms = 1e30f;
+  int best = saved_variant, rc = TWS_OK;
+  for (int v = 0; v < batch_variant_count() && rc == TWS_OK; ++v) {
+    float vbest = 1e30f;
+    for (int rep = 0; rep < 2 && rc == TWS_OK; ++rep) {
+      restore();
+      b->variant = v;
+      cudaEventRecord(e0, b->stream);
+      rc = batch_advance(b, std::vector<int>(n, steps));
+      cudaEventRecord(e1, b->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess) rc = TWS_ERR_CUDA;
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      vbest = std::min(vbest, ms);
+    }
+    if (vbest < best_ms) {
+      best_ms = vbest;
+      best = v;
+    }
+  }
+  restore();
+  for (int i = 0; i < n; ++i) {
+    cudaFreeAsync(saved[i].d, b->stream);
+    cudaFreeAsync(saved[i].f, b->stream);
+    cudaFreeAsync(saved[i].v, b->stream);
+  }
+  cudaStreamSynchronize(b->stream);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->variant = rc == TWS_OK ? best : saved_variant;
+  if (chosen) *chosen = b->variant;
+  return rc;
+}
+
+TWS_API int tws_batch_sync(tws_batch* b) {
+  if (!b) return TWS_ERR_INVALID;
+  if (cudaStreamSynchronize(b->stream) != cudaSuccess) return bfail(b, TWS_ERR_CUDA, "batch sync");
+  for (tws_grid* g : b->grids) {
+    const int rc = tws_sync(g);
+    if (rc != TWS_OK) return bfail(b, rc, g->last_error);
+  }
+  return TWS_OK;
+}
+
+TWS_API void* tws_batch_stream(tws_batch* b) { return b ? (void*)b->stream : nullptr; }
+
+TWS_API const char* tws_batch_last_error(tws_batch* b) {
+  return b ? b->last_error.c_str() : "null batch";
+}
+
+TWS_API int tws_batch_stats(tws_batch* b, uint64_t* chains, uint64_t* graph_launches) {
+  if (!b) return TWS_ERR_INVALID;
+  if (chains) *chains = b->chains;
+  if (graph_launches) *graph_launches = b->graph_launches;
   return TWS_OK;
 }
 

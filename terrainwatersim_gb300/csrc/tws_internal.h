@@ -51,6 +51,33 @@ struct StepVariant {
 
 enum : int { kKindTile = 0, kKindStream = 1 };
 
+// One member grid of a batch as the batched kernel reads it from device
+// memory: its tensor maps (for both ping-pong buffers), its step arguments and
+// its buffers.  64-byte aligned so the tensor maps inside are aligned.
+struct alignas(64) BatchGrid {
+  CUtensorMap tm_b;
+  CUtensorMap tm_d[2];
+  CUtensorMap tm_f[2];
+  StepArgs a;     // W, H, pitch, constants, sources, flux scale, error word
+  float* d[2];
+  void* f[2];
+  float2* v;
+  int cur;        // buffer holding the state when the chain starts
+  int launches;   // launches of this chain that advance this grid
+  int tiles_x;
+  int pad_;
+};
+
+// Batched kernel variants (K steps per launch, tile) and their launcher:
+// `hdr` = {number of grids}, `unit_base[g]` = first work unit (tile) of grid g,
+// unit_base[ngrids] = total units.  Launch `launch_idx` of a chain advances
+// grid g iff launch_idx < grids[g].launches.
+int batch_variant_count();
+void batch_variant_info(int i, int* k, int* tx, int* ty, int* step_variant);
+cudaError_t prepare_batch_variant(int variant, int flux_storage);  // outside any capture
+cudaError_t launch_batch_step(int variant, int flux_storage, const BatchGrid* grids,
+                              const int* unit_base, const int* hdr, int launch_idx, cudaStream_t s);
+
 // Device error codes written to StepArgs::err.
 enum : int { kDevErrNone = 0, kDevErrWaitTimeout = 1 };
 

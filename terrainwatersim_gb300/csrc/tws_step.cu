@@ -164,9 +164,10 @@ __device__ __forceinline__ void issue_tile(unsigned char* st, uint64_t* bar,
 
 // K steps of one tile whose loads have landed in (sb, sd, sf-or-staging).
 template <int K, int TX, int TY, bool F16, int STAGES>
-__device__ __forceinline__ void process_tile(const StepArgs& a, int x0, int y0, uint32_t mask,
-                                             float* sb, float* sd, float* sh, float4* sf,
-                                             const unsigned char* staging) {
+__device__ __forceinline__ void process_tile(const StepArgs& a, float* __restrict__ d_out,
+                                             void* __restrict__ f_out, float2* __restrict__ v_out,
+                                             int x0, int y0, uint32_t mask, float* sb, float* sd,
+                                             float* sh, float4* sf, const unsigned char* staging) {
   using T = Tile<K, TX, TY, F16, STAGES>;
   const int tid = threadIdx.x;
   const int W = a.W, H = a.H;
@@ -268,7 +269,7 @@ __device__ __forceinline__ void process_tile(const StepArgs& a, int x0, int y0, 
         const float dn = max0(fadd(sd[bidx], fmul(fsub(in, out), a.c)));
         if (s == K - 1) {
           const size_t g = (size_t)gy * a.pitch + gx;
-          a.d_out[g] = dn;
+          d_out[g] = dn;
           if (F16) {
             const __half2 lo =
                 __floats2half2_rn(fmul(fc.x, a.flux_scale), fmul(fc.y, a.flux_scale));
@@ -277,11 +278,11 @@ __device__ __forceinline__ void process_tile(const StepArgs& a, int x0, int y0, 
             uint2 packed;
             packed.x = *reinterpret_cast<const uint32_t*>(&lo);
             packed.y = *reinterpret_cast<const uint32_t*>(&hi);
-            reinterpret_cast<uint2*>(a.f_out)[g] = packed;
+            reinterpret_cast<uint2*>(f_out)[g] = packed;
           } else {
-            reinterpret_cast<float4*>(a.f_out)[g] = fc;
+            reinterpret_cast<float4*>(f_out)[g] = fc;
           }
-          a.v_out[g] = make_float2(fsub(fsub(X1, fc.x), fsub(X0, fc.y)),
+          v_out[g] = make_float2(fsub(fsub(X1, fc.x), fsub(X0, fc.y)),
                                    fsub(fsub(Y1, fc.z), fsub(Y0, fc.w)));
         } else {
           const float dnext = mask ? add_sources(dn, gx, gy, a, mask) : dn;
@@ -352,7 +353,8 @@ __global__ void __launch_bounds__(kThreads)
     const bool ok = wait_bounded(&bars[s], parity, a.err);
     if (__syncthreads_or(!ok)) return;  // every thread leaves together on a time-out
 
-    process_tile<K, TX, TY, F16, STAGES>(a, x0, y0, mask, sb, sd, sh, sf, st + T::ST_F);
+    process_tile<K, TX, TY, F16, STAGES>(a, a.d_out, a.f_out, a.v_out, x0, y0, mask, sb, sd, sh,
+                                         sf, st + T::ST_F);
     __syncthreads();  // stage s, h and the F16 working copy are free again
 
     if (tid == 0) {
@@ -363,6 +365,85 @@ __global__ void __launch_bounds__(kThreads)
                            (tn / tiles_x) * TY);
       }
     }
+  }
+}
+
+// ---- the batched kernel ------------------------------------------------------
+// Makes the tensor-map proxy observe the current contents of a tensor map in
+// global memory (the host rewrites a batch's table between chains).
+__device__ __forceinline__ void tensormap_acquire(const void* tm) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(
+                   reinterpret_cast<uint64_t>(tm))
+               : "memory");
+}
+
+// Many grids of different sizes advance in one launch.  Work units are the
+// tiles of every member grid, numbered grid by grid (unit_base); persistent
+// CTAs stride through them, find their grid by binary search, load the tile
+// through that grid's tensor maps and run the same per-tile steps as
+// step_kernel.  Launch `launch_idx` of a chain skips grids that have taken
+// all their launches, so grids with different step counts share a chain.
+template <int K, int TX, int TY, bool F16>
+__global__ void __launch_bounds__(kThreads, 6)
+    batch_kernel(const BatchGrid* __restrict__ grids, const int* __restrict__ unit_base,
+                 const int* __restrict__ hdr, int launch_idx) {
+  using T = Tile<K, TX, TY, F16, 1>;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~static_cast<uintptr_t>(127));
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + T::OFF_BAR);
+  float* sb = reinterpret_cast<float*>(smem + T::ST_B);
+  float* sd = reinterpret_cast<float*>(smem + T::ST_D);
+  float* sh = T::H_ALIAS ? sb : reinterpret_cast<float*>(smem + T::OFF_H);
+  float4* sf = F16 ? reinterpret_cast<float4*>(smem + T::OFF_F16)
+                   : reinterpret_cast<float4*>(smem + T::ST_F);
+  const int tid = threadIdx.x;
+  const int ngrids = hdr[0];
+  const int total = unit_base[ngrids];
+
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  uint32_t it = 0;
+  for (int u = blockIdx.x; u < total; u += gridDim.x) {
+    int lo = 0, hi = ngrids - 1;  // last grid whose first unit is <= u
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(unit_base + mid) <= u) lo = mid;
+      else hi = mid - 1;
+    }
+    const BatchGrid& G = grids[lo];
+    if (launch_idx >= G.launches) continue;
+    const int t = u - __ldg(unit_base + lo);
+    const int x0 = (t % G.tiles_x) * TX, y0 = (t / G.tiles_x) * TY;
+    const int p = (G.cur + launch_idx) & 1;
+    const StepArgs& a = G.a;
+
+    if (tid == 0) {
+      tensormap_acquire(&G.tm_b);
+      tensormap_acquire(&G.tm_d[p]);
+      tensormap_acquire(&G.tm_f[p]);
+      issue_tile<T, F16>(smem, bar, &G.tm_b, &G.tm_d[p], &G.tm_f[p], x0, y0);
+    }
+    uint32_t mask = 0;
+#pragma unroll
+    for (int k = 0; k < TWS_MAX_SOURCES; ++k) {
+      if (k < a.nsrc) {
+        const DevSource& src = a.src[k];
+        if (src.bx1 >= x0 - T::HX && src.bx0 < x0 + TX + T::HX && src.by1 >= y0 - T::HY &&
+            src.by0 < y0 + TY + T::HY)
+          mask |= 1u << k;
+      }
+    }
+    const bool ok = wait_bounded(bar, it & 1u, a.err);
+    ++it;
+    if (__syncthreads_or(!ok)) return;
+    process_tile<K, TX, TY, F16, 1>(a, G.d[p ^ 1], G.f[p ^ 1], G.v, x0, y0, mask, sb, sd, sh, sf,
+                                    smem + T::ST_F);
+    __syncthreads();  // the tile buffers are free again
   }
 }
 
@@ -574,6 +655,102 @@ cudaError_t launch_step(int variant, int flux_storage, const CUtensorMap* tm_b,
   }
   auto kfn = reinterpret_cast<KernelFn>(const_cast<void*>(fn));
   kfn<<<(unsigned)blocks, kThreads, smem, s>>>(*tm_b, *tm_d, *tm_f, a);
+  count_launch();
+  return cudaGetLastError();
+}
+
+// ---- batched variants ---------------------------------------------------------
+namespace {
+
+using BatchFn = void (*)(const BatchGrid*, const int*, const int*, int);
+
+struct BatchEntry {
+  int k, tx, ty, step_variant;  // step_variant: the single-grid variant with the same boxes
+  const void* fn[2];
+  size_t smem[2];
+  int ctas_per_sm[2] = {0, 0};
+  bool set[2] = {false, false};
+};
+
+template <int K, int TX, int TY>
+BatchEntry make_batch_entry(int step_variant) {
+  BatchEntry e;
+  e.k = K;
+  e.tx = TX;
+  e.ty = TY;
+  e.step_variant = step_variant;
+  e.fn[TWS_FLUX_F32] = reinterpret_cast<const void*>(&batch_kernel<K, TX, TY, false>);
+  e.fn[TWS_FLUX_F16] = reinterpret_cast<const void*>(&batch_kernel<K, TX, TY, true>);
+  e.smem[TWS_FLUX_F32] = Tile<K, TX, TY, false, 1>::SMEM;
+  e.smem[TWS_FLUX_F16] = Tile<K, TX, TY, true, 1>::SMEM;
+  return e;
+}
+
+struct BatchTable {
+  BatchEntry e[8];
+  int n = 0;
+  std::mutex mu;
+  BatchTable() {
+    e[n++] = make_batch_entry<1, 32, 32>(0);
+    e[n++] = make_batch_entry<2, 32, 32>(10);
+    e[n++] = make_batch_entry<1, 64, 16>(4);
+    e[n++] = make_batch_entry<2, 64, 16>(1);
+  }
+};
+
+BatchTable& batch_table() {
+  static BatchTable t;
+  return t;
+}
+
+}  // namespace
+
+int batch_variant_count() { return batch_table().n; }
+
+void batch_variant_info(int i, int* k, int* tx, int* ty, int* step_variant) {
+  const BatchEntry& e = batch_table().e[i];
+  if (k) *k = e.k;
+  if (tx) *tx = e.tx;
+  if (ty) *ty = e.ty;
+  if (step_variant) *step_variant = e.step_variant;
+}
+
+cudaError_t prepare_batch_variant(int variant, int flux_storage) {
+  BatchTable& t = batch_table();
+  if (variant < 0 || variant >= t.n) return cudaErrorInvalidValue;
+  const int fs = flux_storage == TWS_FLUX_F16 ? TWS_FLUX_F16 : TWS_FLUX_F32;
+  BatchEntry& e = t.e[variant];
+  std::lock_guard<std::mutex> lk(t.mu);
+  if (!e.set[fs]) {
+    cudaError_t err =
+        cudaFuncSetAttribute(e.fn[fs], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e.smem[fs]);
+    if (err != cudaSuccess) return err;
+    int n = 0;
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, e.fn[fs], kThreads, e.smem[fs]);
+    if (err != cudaSuccess) return err;
+    e.ctas_per_sm[fs] = n > 0 ? n : 1;
+    e.set[fs] = true;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t launch_batch_step(int variant, int flux_storage, const BatchGrid* grids,
+                              const int* unit_base, const int* hdr, int launch_idx,
+                              cudaStream_t s) {
+  cudaError_t err = prepare_batch_variant(variant, flux_storage);
+  if (err != cudaSuccess) return err;
+  const int fs = flux_storage == TWS_FLUX_F16 ? TWS_FLUX_F16 : TWS_FLUX_F32;
+  BatchEntry& e = batch_table().e[variant];
+  const int ctas = e.ctas_per_sm[fs];
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  auto fn = reinterpret_cast<BatchFn>(const_cast<void*>(e.fn[fs]));
+  fn<<<sms * ctas, kThreads, e.smem[fs], s>>>(grids, unit_base, hdr, launch_idx);
   count_launch();
   return cudaGetLastError();
 }

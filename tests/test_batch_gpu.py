@@ -1,0 +1,161 @@
+"""GPU tests of batches: many uneven grids advanced by one persistent launch
+per step (chains replayed from CUDA graphs) give, grid by grid, the same bits
+as the oracle -- alone or in the mix, with grids joining and leaving between
+calls, with per-grid step counts, with graphs on or off."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import assert_bitexact
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def tws():
+    import terrainwatersim_gb300 as t
+    t.lib()
+    return t
+
+
+# uneven grids: ragged sizes, both borders, different constants and sources
+SPECS = [
+    # (W, H, boundary, damping, seed, rain radius, rain rate)
+    (96, 80, 0, 0.998, 1, 10, 0.02),
+    (257, 33, 1, 0.99, 2, 6, 0.05),
+    (33, 190, 0, 0.995, 3, 5, 0.01),
+    (1, 45, 0, 0.998, 4, 0, 0.0),
+    (128, 128, 1, 0.97, 5, 20, 0.005),
+    (70, 7, 0, 0.998, 6, 3, 0.1),
+]
+
+
+def make_grid(tws, oracle, spec, flux_storage=0):
+    W, H, boundary, damping, seed, r, rate = spec
+    p = tws.params_physical(0.02, 9.81, 1.0, 1.0, damping, boundary)
+    b, d = oracle.terrain(seed, W, H, 40.0, 15.0)
+    g = tws.Grid(W, H, p, flux_storage)
+    g.upload(b, d)
+    srcs = tws.rain_disks(seed, W, H, r, rate, 1) if r > 0 else []
+    g.set_sources(srcs)
+    return g, (b, d, p, srcs)
+
+
+def oracle_state(oracle, setup, steps, flux_scale=0.0):
+    b, d, p, srcs = setup
+    H, W = b.shape
+    d = d.copy()
+    f = np.zeros((H, W, 4), np.float32)
+    v = np.zeros((H, W, 2), np.float32)
+    kf, ka, c = p.as_tuple()
+    oracle.step_f32(b.copy(), d, f, v, kf, ka, c, p.boundary,
+                    [(s[0], s[1], s[2], s[3], s[4]) for s in srcs], nsteps=steps,
+                    flux_scale=flux_scale)
+    return d, f, v
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+def test_batch_variants_match_oracle_per_grid(tws, oracle, variant):
+    grids, setups = zip(*[make_grid(tws, oracle, s) for s in SPECS])
+    with tws.Batch() as batch:
+        for g in grids:
+            batch.add(g)
+        batch.set_variant(variant)
+        batch.step(37)  # two full chains and a partial one; odd for K = 2
+        batch.sync()
+        for g, setup in zip(grids, setups):
+            od, of, ov = oracle_state(oracle, setup, 37)
+            gd, gf, gv = g.download()
+            assert_bitexact(gd, od, f"depth {g.width}x{g.height}")
+            assert_bitexact(gf, of, f"flux {g.width}x{g.height}")
+            assert_bitexact(gv, ov, f"velocity {g.width}x{g.height}")
+    for g in grids:
+        g.close()
+
+
+@pytest.mark.parametrize("graphs", [True, False])
+def test_batch_step_each_and_join_leave(tws, oracle, graphs):
+    """Grids join and leave between calls and advance by their own counts;
+    each result equals the grid alone."""
+    made = [make_grid(tws, oracle, s) for s in SPECS]
+    grids = [m[0] for m in made]
+    setups = [m[1] for m in made]
+    done = {}
+    with tws.Batch() as batch:
+        batch.use_graphs(graphs)
+        for g in grids[:3]:
+            batch.add(g)
+        batch.step_each([5, 21, 0])
+        done[0] = 5
+        batch.add(grids[3])
+        batch.add(grids[4])
+        batch.step_each([0, 11, 40, 17, 3])
+        batch.remove(grids[0])          # leaves after 5 steps
+        batch.add(grids[5])
+        batch.step_each([1, 2, 3, 4, 16])
+        batch.sync()
+        totals = {1: 21 + 11 + 1, 2: 0 + 40 + 2, 3: 17 + 3, 4: 3 + 4, 5: 16}
+        done.update(totals)
+        chains, replayed = batch.stats()
+        assert chains > 0
+        assert (replayed > 0) == graphs
+    for i, g in enumerate(grids):
+        od, of, ov = oracle_state(oracle, setups[i], done[i])
+        gd, gf, gv = g.download()
+        assert_bitexact(gd, od, f"depth grid {i}")
+        assert_bitexact(gf, of, f"flux grid {i}")
+        assert_bitexact(gv, ov, f"velocity grid {i}")
+        g.close()
+
+
+def test_batch_fp16_storage_matches_oracle(tws, oracle):
+    made = [make_grid(tws, oracle, s, flux_storage=tws.FLUX_F16) for s in SPECS[:4]]
+    with tws.Batch(tws.FLUX_F16) as batch:
+        for g, _ in made:
+            batch.add(g)
+        batch.step(24)
+        batch.sync()
+        for g, setup in made:
+            scale = g.buffers().flux_scale
+            od, of, ov = oracle_state(oracle, setup, 24, flux_scale=scale)
+            gd, gf, gv = g.download()
+            assert_bitexact(gd, od, "depth")
+            assert_bitexact(gf, of, "flux")
+            assert_bitexact(gv, ov, "velocity")
+    for g, _ in made:
+        g.close()
+
+
+def test_batch_rejects_mixed_storage_and_double_membership(tws, oracle):
+    g32, _ = make_grid(tws, oracle, SPECS[0])
+    g16, _ = make_grid(tws, oracle, SPECS[1], flux_storage=tws.FLUX_F16)
+    with tws.Batch() as b1, tws.Batch() as b2:
+        b1.add(g32)
+        with pytest.raises(tws.TwsError):
+            b1.add(g16)
+        with pytest.raises(tws.TwsError):
+            b2.add(g32)
+        with pytest.raises(tws.TwsError):
+            b1.step_each([1, 2])
+    g32.close()
+    g16.close()
+
+
+def test_batch_autotune_preserves_state(tws, oracle):
+    made = [make_grid(tws, oracle, s) for s in SPECS]
+    with tws.Batch() as batch:
+        for g, _ in made:
+            batch.add(g)
+        batch.step(3)
+        v = batch.autotune(16)
+        assert 0 <= v < len(tws.batch_variants())
+        batch.step(5)
+        batch.sync()
+        for g, setup in made:
+            od, of, ov = oracle_state(oracle, setup, 8)
+            gd, gf, gv = g.download()
+            assert_bitexact(gd, od, "depth")
+            assert_bitexact(gf, of, "flux")
+    for g, _ in made:
+        g.close()

@@ -60,6 +60,11 @@ def parse():
     ap.add_argument("--flux", choices=["f32", "f16"], default="f32")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--config", choices=["c1", "c2", "c3", "c4", "c5"], default="c2",
+                    help="c2 (default): the 4096^2 headline; c1: 256^2; c3: 64 uneven grids "
+                         "batched; c4: 16384^2 FP16 flux; c5: serving loop")
+    ap.add_argument("--requests", type=int, default=2000, help="c5: requests in the stream")
+    ap.add_argument("--max-steps", type=int, default=20000, help="c5: largest step count")
     return ap.parse_args()
 
 
@@ -471,8 +476,358 @@ def run_reference(args):
     }
 
 
+# ------------------------------------------------------------------ other configurations
+
+def _events(torch, stream, n):
+    return [torch.cuda.Event(enable_timing=True) for _ in range(n)]
+
+
+def run_c1(args):
+    """256^2, closed walls, rain r=16, 1000 steps: throughput, per-step latency,
+    parity with the FP32 oracle and drift against the FP64 oracle."""
+    import torch
+
+    import terrainwatersim_gb300 as tws
+    from oracle import oracle as O
+
+    W = H = 256
+    steps = 1000
+    p = tws.params_physical(0.02, 9.81, 1.0, 1.0, 0.998, tws.BOUNDARY_CLOSED)
+    rain = tws.rain_disks(2026, W, H, 16, 0.01, 1)
+    stream = torch.cuda.Stream()
+    g = tws.Grid(W, H, p, stream=stream.cuda_stream)
+    g.set_sources(rain)
+    g.generate_scene(2026, 40.0, 15.0)
+    tuned = g.autotune(24)
+    g.generate_scene(2026, 40.0, 15.0)
+    g.step(50)  # warm-up
+    g.generate_scene(2026, 40.0, 15.0)
+    torch.cuda.synchronize()
+    ev = _events(torch, stream, steps + 1)
+    ev[0].record(stream)
+    for i in range(steps):
+        g.step(1)
+        ev[i + 1].record(stream)
+    torch.cuda.synchronize()
+    per = sorted(ev[i].elapsed_time(ev[i + 1]) * 1e3 for i in range(steps))
+    total = ev[0].elapsed_time(ev[steps]) / 1e3
+    d, f, v = g.download()
+    vol = g.volume()
+    b, od = O.terrain(2026, W, H, 40.0, 15.0)
+    of = np.zeros((H, W, 4), np.float32)
+    ov = np.zeros((H, W, 2), np.float32)
+    src = [(s[0], s[1], s[2], s[3], s[4]) for s in rain]
+    kf, ka, c = p.as_tuple()
+    O.step_f32(b, od, of, ov, kf, ka, c, O.BOUNDARY_CLOSED, src, nsteps=steps)
+    b64, d64 = O.terrain(2026, W, H, 40.0, 15.0)
+    b64, d64 = b64.astype(np.float64), d64.astype(np.float64)
+    f64 = np.zeros((H, W, 4), np.float64)
+    k64 = O.params_physical()
+    O.step_f64(b64, d64, f64, None, *k64, O.BOUNDARY_CLOSED,
+               [(s[0], s[1], s[2], s[3], 0.01) for s in rain], nsteps=steps)
+    v64 = O.volume(d64)
+    g.close()
+    return {
+        "config": "256x256 FP32, closed walls, rain r=16 +0.01 m/step, 1000 steps, one launch per step",
+        "gcell_steps_per_s": round(W * H * steps / total / 1e9, 3),
+        "step_us_p50": round(per[len(per) // 2], 2),
+        "step_us_p99": round(per[int(0.99 * len(per))], 2),
+        "variant": tuned,
+        "bitexact_vs_fp32_oracle": bool(np.array_equal(d.view(np.uint32), od.view(np.uint32))
+                                        and np.array_equal(f.view(np.uint32), of.view(np.uint32))
+                                        and np.array_equal(v.view(np.uint32), ov.view(np.uint32))),
+        "rel_volume_diff_vs_fp32_oracle": abs(vol - O.volume(od)) / O.volume(od),
+        "max_abs_depth_err_vs_fp64": float(np.abs(d - d64).max()),
+        "rel_volume_drift_vs_fp64": abs(vol - v64) / v64,
+    }
+
+
+def c3_workload(n=64, seed=2026):
+    """64 grids: side log-uniform in [128, 2048] rounded to 32, aspect U[1, 4],
+    own terrain seed, fill U[8, 20] m, rain U[0.002, 0.02] m/step on one disk of
+    radius 16."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        side = int(round(np.exp(rng.uniform(np.log(128), np.log(2048))) / 32)) * 32
+        aspect = rng.uniform(1.0, 4.0)
+        other = max(32, int(round(side * aspect / 32)) * 32)
+        W, H = (side, other) if i % 2 == 0 else (other, side)
+        out.append(dict(W=W, H=H, seed=10000 + i, fill=float(rng.uniform(8, 20)),
+                        rate=float(rng.uniform(0.002, 0.02)), radius=16))
+    return out
+
+
+def run_c3(args):
+    import torch
+
+    import terrainwatersim_gb300 as tws
+    from oracle import oracle as O
+
+    steps = 2000
+    work = c3_workload()
+    p = tws.params_physical(0.02, 9.81, 1.0, 1.0, 0.998, tws.BOUNDARY_CLOSED)
+    grids = []
+    for w in work:
+        g = tws.Grid(w["W"], w["H"], p)
+        g.set_sources(tws.rain_disks(w["seed"], w["W"], w["H"], w["radius"], w["rate"], 1))
+        grids.append(g)
+    cells = sum(w["W"] * w["H"] for w in work)
+
+    def reset():
+        for g, w in zip(grids, work):
+            g.generate_scene(w["seed"], 40.0, w["fill"])
+        for g in grids:
+            g.sync()
+
+    # per-grid plain launches: every grid advanced on its own, one launch per step
+    reset()
+    for g in grids:
+        g.set_variant(0)
+        g.step(16)
+    torch.cuda.synchronize()
+    reset()
+    t0 = time.perf_counter()
+    for g in grids:  # one grid at a time
+        g.step(steps)
+        g.sync()
+    plain_s = time.perf_counter() - t0
+    reset()
+    t0 = time.perf_counter()
+    for g in grids:  # every grid on its own stream, all in flight together
+        g.step(steps)
+    for g in grids:
+        g.sync()
+    plain_streams_s = time.perf_counter() - t0
+
+    # batched: one persistent launch per step over all 64 grids, graph chains of 16
+    reset()
+    batch = tws.Batch()
+    for g in grids:
+        batch.add(g)
+    tuned = batch.autotune(32)
+    batch.step(32)
+    batch.sync()
+    reset()
+    ev = _events(torch, None, 2)
+    t0 = time.perf_counter()
+    batch.step(steps)
+    batch.sync()
+    batch_s = time.perf_counter() - t0
+    chains, replayed = batch.stats()
+
+    # FP64 oracle on 4 sampled grids (the smallest four, for CPU time)
+    order = sorted(range(len(work)), key=lambda i: work[i]["W"] * work[i]["H"])[:4]
+    checks = []
+    for i in order:
+        w, g = work[i], grids[i]
+        d, _, _ = g.download(flux=False, velocity=False)
+        vol = float(np.sum(d, dtype=np.float64))
+        b64, d64 = O.terrain(w["seed"], w["W"], w["H"], 40.0, w["fill"])
+        b64, d64 = b64.astype(np.float64), d64.astype(np.float64)
+        f64 = np.zeros((w["H"], w["W"], 4), np.float64)
+        (cx, cy), = O.rain_centers(w["seed"], w["W"], w["H"], w["radius"], 1)
+        O.step_f64(b64, d64, f64, None, *O.params_physical(), O.BOUNDARY_CLOSED,
+                   [(O.SOURCE_DISK, cx, cy, w["radius"], w["rate"])], nsteps=steps)
+        v64 = O.volume(d64)
+        checks.append({"grid": [w["W"], w["H"]],
+                       "max_abs_depth_err_vs_fp64": float(np.abs(d - d64).max()),
+                       "rel_volume_drift_vs_fp64": abs(vol - v64) / v64})
+    batch.close()
+    for g in grids:
+        g.close()
+    del ev
+    return {
+        "config": "64 uneven grids (side log-uniform 128-2048, aspect 1-4), 2000 steps, "
+                  "closed walls, per-grid seed/fill/rain",
+        "cells": cells,
+        "batched_gcell_steps_per_s": round(cells * steps / batch_s / 1e9, 3),
+        "per_grid_plain_gcell_steps_per_s": round(cells * steps / plain_s / 1e9, 3),
+        "per_grid_plain_concurrent_streams_gcell_steps_per_s":
+            round(cells * steps / plain_streams_s / 1e9, 3),
+        "speedup_vs_one_grid_at_a_time": round(plain_s / batch_s, 3),
+        "speedup_vs_concurrent_streams": round(plain_streams_s / batch_s, 3),
+        "batched_variant": tws.batch_variants()[tuned],
+        "chains": chains, "graph_replays": replayed,
+        "fp64_checks": checks,
+    }
+
+
+def run_c4(args):
+    """16384^2, 8 rain disks r=128, FP16 flux storage vs all-FP32, 5000 steps.
+    Volume drift against the exact FP64 bookkeeping (initial FP64 volume plus
+    the rain added); depth error against the FP64 oracle on a 1024^2 window
+    after a reduced run whose domain of dependence fits an oracle crop."""
+    import torch
+
+    import terrainwatersim_gb300 as tws
+    from oracle import oracle as O
+
+    N = args.size if args.size != W_DEFAULT else 16384
+    steps = 5000
+    p = tws.params_physical(0.02, 9.81, 1.0, 1.0, 0.998, tws.BOUNDARY_CLOSED)
+    rain = tws.rain_disks(2026, N, N, 128, 0.01, 8)
+    out = {"config": f"{N}x{N}, 8 rain disks r=128 +0.01 m/step, closed walls, {steps} steps"}
+    disk_cells = 0
+    for s in rain:
+        r = int(s[3])
+        yy, xx = np.mgrid[-r:r + 1, -r:r + 1]
+        disk_cells += int(np.count_nonzero(xx * xx + yy * yy <= r * r))
+    for name, fs in (("fp16_flux", tws.FLUX_F16), ("fp32", tws.FLUX_F32)):
+        g = tws.Grid(N, N, p, fs)
+        g.set_sources(rain)
+        g.generate_scene(2026, 40.0, 15.0)
+        v0 = g.volume()
+        tuned = g.autotune(24)
+        g.generate_scene(2026, 40.0, 15.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g.step(steps)
+        g.sync()
+        secs = time.perf_counter() - t0
+        vol = g.volume()
+        exact = v0 + steps * 0.01 * disk_cells
+        bpc = BYTES_PER_CELL_STEP_F16 if fs == tws.FLUX_F16 else BYTES_PER_CELL_STEP_F32
+        out[name] = {"gcell_steps_per_s": round(N * N * steps / secs / 1e9, 3),
+                     "effective_gbs": round(bpc * N * N * steps / secs / 1e9, 1),
+                     "variant": tuned, "flux_scale": g.buffers().flux_scale,
+                     "rel_volume_drift_vs_fp64_bookkeeping": abs(vol - exact) / exact}
+        g.close()
+        torch.cuda.empty_cache()
+    # depth error on a 1024^2 window: GPU (full grid) vs FP64 oracle (crop)
+    short, win = 200, 1024
+    margin = 2 * short + 8
+    x0 = y0 = N // 2 - win // 2
+    cx0, cy0, cw = x0 - margin, y0 - margin, win + 2 * margin
+    for name, fs in (("fp16_flux", tws.FLUX_F16), ("fp32", tws.FLUX_F32)):
+        g = tws.Grid(N, N, p, fs)
+        g.set_sources(rain)
+        g.generate_scene(2026, 40.0, 15.0)
+        g.step(short)
+        d, _, _ = g.download(flux=False, velocity=False)
+        g.close()
+        b, d0 = O.terrain(2026, N, N, 40.0, 15.0)
+        b64 = np.ascontiguousarray(b[cy0:cy0 + cw, cx0:cx0 + cw]).astype(np.float64)
+        d64 = np.ascontiguousarray(d0[cy0:cy0 + cw, cx0:cx0 + cw]).astype(np.float64)
+        del b, d0
+        f64 = np.zeros((cw, cw, 4), np.float64)
+        srcs = [(O.SOURCE_DISK, s[1] - cx0, s[2] - cy0, s[3], 0.01) for s in rain]
+        O.step_f64(b64, d64, f64, None, *O.params_physical(), O.BOUNDARY_CLOSED, srcs,
+                   nsteps=short)
+        ref = d64[margin:margin + win, margin:margin + win]
+        gw = d[y0:y0 + win, x0:x0 + win]
+        out[name]["window_steps"] = short
+        out[name]["window_max_abs_depth_err_vs_fp64"] = float(np.abs(gw - ref).max())
+        out[name]["window_rel_max_depth_err_vs_fp64"] = float(np.abs(gw - ref).max()
+                                                               / max(1e-30, np.abs(ref).max()))
+    return out
+
+
+def c5_workload(n, max_steps, seed=2026):
+    """Requests: side log-uniform [64, 4096], aspect U[1, 2], own terrain seed,
+    fill U[8, 20] m, one rain disk (radius min(W, H)/32, at least 4 cells,
+    +0.01 m/step), steps log-uniform [100, max_steps]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        side = int(round(np.exp(rng.uniform(np.log(64), np.log(4096)))))
+        other = int(round(side * rng.uniform(1.0, 2.0)))
+        W, H = (side, other) if i % 2 == 0 else (other, side)
+        steps = int(round(np.exp(rng.uniform(np.log(100), np.log(max_steps)))))
+        out.append(dict(W=W, H=H, seed=50000 + i, fill=float(rng.uniform(8, 20)),
+                        radius=max(4, min(W, H) // 32), rate=0.01, steps=steps))
+    return out
+
+
+def run_c5(args):
+    """Serving loop vs serial plain-kernel execution of the same request stream."""
+    import torch
+
+    import terrainwatersim_gb300 as tws
+    from terrainwatersim_gb300 import serve
+
+    n = args.requests
+    work = c5_workload(n, args.max_steps)
+    total_cell_steps = float(sum(w["W"] * w["H"] * w["steps"] for w in work))
+    p = tws.params_physical(0.02, 9.81, 1.0, 1.0, 0.998, tws.BOUNDARY_CLOSED)
+
+    # capacity: the batched FP16 path on a large grid (cell-steps per second)
+    g = tws.Grid(4096, 4096, p, tws.FLUX_F16)
+    g.generate_scene(1, 40.0, 15.0)
+    g.step(32)
+    g.sync()
+    t0 = time.perf_counter()
+    g.step(400)
+    g.sync()
+    capacity = 4096 * 4096 * 400 / (time.perf_counter() - t0)
+    g.close()
+    load = 0.7
+    rate = load * capacity / (total_cell_steps / n)  # requests per second
+    rng = np.random.default_rng(7)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
+    arrivals -= arrivals[0]
+
+    # exact FP64 bookkeeping of the final volumes: initial volume + rain added
+    expected = []
+    for w in work:
+        gg = tws.Grid(w["W"], w["H"], p, tws.FLUX_F32)
+        gg.generate_scene(w["seed"], 40.0, w["fill"])
+        v0 = gg.volume()
+        gg.close()
+        r = w["radius"]
+        yy, xx = np.mgrid[-r:r + 1, -r:r + 1]
+        ncells = int(np.count_nonzero(xx * xx + yy * yy <= r * r))
+        expected.append(v0 + w["steps"] * float(np.float32(w["rate"])) * ncells)
+    torch.cuda.empty_cache()
+
+    def requests():
+        for i, w in enumerate(work):
+            src = tws.rain_disks(w["seed"], w["W"], w["H"], w["radius"], w["rate"], 1)
+            yield serve.make_request(i, w["W"], w["H"], w["seed"], w["fill"], p, src, w["steps"],
+                                     float(arrivals[i]))
+
+    out = {"config": f"{n} Poisson requests, side log-uniform 64-4096, aspect 1-2, steps "
+                     f"log-uniform 100-{args.max_steps}, one rain disk each, closed walls, "
+                     f"arrival rate for {int(load * 100)}% load of the measured FP16 capacity",
+           "requests": n, "total_cell_steps": total_cell_steps,
+           "capacity_gcell_steps_per_s": round(capacity / 1e9, 3),
+           "arrival_rate_per_s": round(rate, 3), "arrival_span_s": round(float(arrivals[-1]), 3)}
+    for name, fs, serial in (("served_fp16_batched", tws.FLUX_F16, False),
+                             ("serial_fp32_plain", tws.FLUX_F32, True)):
+        with serve.Server(memory_budget_bytes=120e9, flux_storage=fs) as srv:
+            for r in requests():
+                srv.submit(r)
+            srv.close_submissions()
+            srv.run(serial=serial)
+            res = sorted(srv.results(), key=lambda r: r.id)
+            st = srv.stats()
+        ok = [r for r in res if r.status == 0]
+        lat = np.array([r.latency_s for r in ok])
+        makespan = max(r.done_s for r in ok) - min(r.arrival_s for r in ok)
+        drift = [abs(r.volume - expected[r.id]) / expected[r.id] for r in ok]
+        out[name] = {
+            "completed": len(ok),
+            "aggregate_gcell_steps_per_s": round(st["cell_steps"] / makespan / 1e9, 3),
+            "busy_gcell_steps_per_s": round(st["cell_steps"] / st["seconds"] / 1e9, 3),
+            "makespan_s": round(makespan, 3),
+            "latency_s_p50": round(float(np.percentile(lat, 50)), 4),
+            "latency_s_p95": round(float(np.percentile(lat, 95)), 4),
+            "latency_s_p99": round(float(np.percentile(lat, 99)), 4),
+            "peak_resident_gb": round(st["peak_bytes"] / 1e9, 3),
+            "chains": st["chains"],
+            "max_rel_volume_drift_vs_fp64_bookkeeping": float(max(drift)),
+        }
+    out["aggregate_speedup"] = round(out["served_fp16_batched"]["aggregate_gcell_steps_per_s"]
+                                     / out["serial_fp32_plain"]["aggregate_gcell_steps_per_s"], 3)
+    return out
+
+
 def main():
     args = parse()
+    if args.config != "c2":
+        res = {"c1": run_c1, "c3": run_c3, "c4": run_c4, "c5": run_c5}[args.config](args)
+        print(json.dumps(res), flush=True)
+        return
     res = run_reference(args) if args.impl == "reference" else run_ours(args)
     if res is not None:
         print(json.dumps(res), flush=True)

@@ -265,6 +265,66 @@ TWS_API const char* tws_batch_last_error(tws_batch* batch);
 /* Chains run and chains replayed from a graph so far. */
 TWS_API int tws_batch_stats(tws_batch* batch, uint64_t* chains, uint64_t* graph_launches);
 
+/* ---- serving loop ----------------------------------------------------------
+ * Requests (a grid size, a synthetic scene, sources, a step count and an
+ * arrival time) are admitted once their arrival time has passed and their
+ * state fits the device-memory budget; admitted grids stay resident and are
+ * advanced together in batch chains (continuous batching: requests join and
+ * leave between chains); a finished grid reports its time to completion and
+ * its FP64 water volume, and its memory is released.  No counterpart in the
+ * reference (an interactive single-grid program). */
+typedef struct tws_server tws_server;
+
+typedef struct tws_server_config {
+  double memory_budget_bytes; /* admission limit on resident grid state       */
+  int flux_storage;           /* TWS_FLUX_* of every request                    */
+  int chain_steps;            /* steps per chain (<= 0: 16)                      */
+  int batch_variant;          /* batched kernel variant; -1: autotune at start  */
+  int keep_grids;             /* 1: finished grids are kept (tws_server_result  */
+                              /*    returns them, the caller destroys them)     */
+} tws_server_config;
+
+typedef struct tws_request {
+  uint64_t id;
+  int width, height;
+  uint64_t seed;       /* scene: tws_generate_scene(seed, height_scale, fill) */
+  float height_scale, fill;
+  tws_sim_params params;
+  int nsources;
+  tws_source sources[TWS_MAX_SOURCES];
+  int steps;
+  double arrival_s;    /* seconds after tws_server_run starts                */
+} tws_request;
+
+typedef struct tws_result {
+  uint64_t id;
+  int status;          /* TWS_OK, or the error that ended the request         */
+  int steps;           /* steps done                                          */
+  double arrival_s, admit_s, done_s; /* seconds after the run started         */
+  double volume;       /* FP64 total water volume at the end                  */
+  tws_grid* grid;      /* keep_grids: the finished grid, else NULL            */
+} tws_result;
+
+TWS_API int tws_server_create(const tws_server_config* config, tws_server** out);
+TWS_API int tws_server_destroy(tws_server* server);
+/* Thread-safe; may be called while tws_server_run is running. */
+TWS_API int tws_server_submit(tws_server* server, const tws_request* request);
+/* No more submissions: tws_server_run returns once everything submitted is done. */
+TWS_API int tws_server_close(tws_server* server);
+/* Runs the loop until the server is closed and idle (call tws_server_close
+ * first, or from another thread).  serial = 1 runs the baseline instead: one
+ * request at a time, in arrival order, through the single-grid path. */
+TWS_API int tws_server_run(tws_server* server, int serial);
+TWS_API int tws_server_result_count(tws_server* server);
+TWS_API int tws_server_result(tws_server* server, int index, tws_result* out);
+/* Totals of the last run: cell-steps done, wall seconds, peak resident bytes,
+ * chains run. */
+TWS_API int tws_server_stats(tws_server* server, double* cell_steps, double* seconds,
+                             double* peak_bytes, uint64_t* chains);
+
+/* Device bytes a grid of this size holds (tws_create's allocations). */
+TWS_API double tws_grid_bytes(int width, int height, int flux_storage);
+
 /* Block the host until the grid's queued work is done; reports a device-side
  * error (TWS_ERR_TIMEOUT) raised by any kernel of this grid. */
 TWS_API int tws_sync(tws_grid* grid);

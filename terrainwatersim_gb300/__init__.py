@@ -129,6 +129,15 @@ def _declare(L):
         "tws_batch_stream": ([vp], vp),
         "tws_batch_last_error": ([vp], C.c_char_p),
         "tws_batch_stats": ([vp, vp, vp], i),
+        "tws_server_create": ([vp, vp], i),
+        "tws_server_destroy": ([vp], i),
+        "tws_server_submit": ([vp, vp], i),
+        "tws_server_close": ([vp], i),
+        "tws_server_run": ([vp, i], i),
+        "tws_server_result_count": ([vp], i),
+        "tws_server_result": ([vp, i, vp], i),
+        "tws_server_stats": ([vp, vp, vp, vp, vp], i),
+        "tws_grid_bytes": ([i, i, i], d),
         "tws_version": ([], C.c_char_p),
     }
     for name, (args, res) in sig.items():

@@ -1033,6 +1033,13 @@ TWS_API const char* tws_batch_last_error(tws_batch* b) {
   return b ? b->last_error.c_str() : "null batch";
 }
 
+TWS_API double tws_grid_bytes(int width, int height, int flux_storage) {
+  if (width < 1 || height < 1) return 0.0;
+  const double cells = (double)((width + 31) / 32 * 32) * height;
+  return cells * (4.0 + 8.0 + 2.0 * flux_bytes_per_cell(flux_storage) + 8.0) +
+         sizeof(double) * (volume_partials_needed() + 1) + sizeof(int);
+}
+
 TWS_API int tws_batch_stats(tws_batch* b, uint64_t* chains, uint64_t* graph_launches) {
   if (!b) return TWS_ERR_INVALID;
   if (chains) *chains = b->chains;

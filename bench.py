@@ -792,10 +792,15 @@ def run_c5(args):
            "requests": n, "total_cell_steps": total_cell_steps,
            "capacity_gcell_steps_per_s": round(capacity / 1e9, 3),
            "arrival_rate_per_s": round(rate, 3), "arrival_span_s": round(float(arrivals[-1]), 3)}
-    for name, fs, serial in (("served_fp16_batched", tws.FLUX_F16, False),
-                             ("serial_fp32_plain", tws.FLUX_F32, True)):
+    runs = (("served_fp16_batched", tws.FLUX_F16, False, True),
+            ("serial_fp32_plain", tws.FLUX_F32, True, True),
+            ("saturated_served_fp16_batched", tws.FLUX_F16, False, False),
+            ("saturated_serial_fp32_plain", tws.FLUX_F32, True, False))
+    for name, fs, serial, poisson in runs:
         with serve.Server(memory_budget_bytes=120e9, flux_storage=fs) as srv:
             for r in requests():
+                if not poisson:  # every request present at the start: capacity
+                    r.arrival_s = 0.0
                 srv.submit(r)
             srv.close_submissions()
             srv.run(serial=serial)
@@ -819,6 +824,9 @@ def run_c5(args):
         }
     out["aggregate_speedup"] = round(out["served_fp16_batched"]["aggregate_gcell_steps_per_s"]
                                      / out["serial_fp32_plain"]["aggregate_gcell_steps_per_s"], 3)
+    out["saturated_speedup"] = round(
+        out["saturated_served_fp16_batched"]["aggregate_gcell_steps_per_s"]
+        / out["saturated_serial_fp32_plain"]["aggregate_gcell_steps_per_s"], 3)
     return out
 
 

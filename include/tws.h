@@ -218,6 +218,34 @@ TWS_API int tws_volume(tws_grid* grid, double* out);
 TWS_API int tws_volume_noalloc(const float* depth, int width, int height, int pitch,
                                double cell_area, double* out, void* stream);
 
+/* ---- what the renderer reads ---------------------------------------------
+ * The water shaders' per-texel arithmetic on the current state, written to
+ * caller-owned device buffers (W x H, tightly packed; any pointer may be
+ * NULL).  Replaces the reads of TerrainInfo and FlowMap in
+ * waterRender.vert:21-23, waterRender.eval:32-35 and waterRender.frag:50-62,
+ * 217, 240-241, 341-346 (neighbours wrap around, as the REPEAT sampler bound
+ * in Terrain.cpp:313 does).  Asynchronous on the grid's stream. */
+typedef struct tws_surface_out {
+  float* height;        /* d + b                                        */
+  float* render_height; /* (d + b) - 0.1, and 10 lower where d < 0.1    */
+  float* normal;        /* 3 floats per cell: normalised (-dhx, 1, -dhz) */
+  float* flow_speed;    /* |flow| of the RG16F flow map                 */
+  float* foam;          /* saturate(|flow|^2 * 0.00004)                  */
+  unsigned char* dry;   /* 1 where d < 0.1                              */
+} tws_surface_out;
+TWS_API int tws_surface(tws_grid* grid, const tws_surface_out* out);
+
+/* The reference's texture layouts in caller-owned device buffers:
+ * terrain_rgba = TerrainData as RGBA32F (r = terrain, g = b = 0.3, a = depth;
+ * Terrain.cpp:216-220), flowmap_rg16f = FlowMap as two IEEE halves per cell
+ * (flowApply.comp:7), and `mip_levels` levels of the 2x2 box-filtered mip
+ * pyramid of TerrainData (Terrain.cpp:273-276), packed level after level in
+ * `mips` (level l is floor(W/2^l) x floor(H/2^l) RGBA32F texels; every level
+ * must be at least 1 x 1).  Any pointer may be NULL (mips need terrain_rgba).
+ * Asynchronous on the grid's stream. */
+TWS_API int tws_export_textures(tws_grid* grid, float* terrain_rgba, uint16_t* flowmap_rg16f,
+                                int mip_levels, float* mips);
+
 /* Copy state to host arrays (each may be NULL).  Flux is returned as 4 floats
  * per cell whatever the storage.  Synchronous. */
 TWS_API int tws_download(tws_grid* grid, float* depth, float* flux, float* velocity);
@@ -278,7 +306,8 @@ typedef struct tws_server tws_server;
 typedef struct tws_server_config {
   double memory_budget_bytes; /* admission limit on resident grid state       */
   int flux_storage;           /* TWS_FLUX_* of every request                    */
-  int chain_steps;            /* steps per chain (<= 0: 16)                      */
+  int chain_steps;            /* steps per chain; <= 0: sized per chain to about */
+                              /* 1.5e9 cell-steps of work (16 to 512 steps)     */
   int batch_variant;          /* batched kernel variant; -1: autotune at start  */
   int keep_grids;             /* 1: finished grids are kept (tws_server_result  */
                               /*    returns them, the caller destroys them)     */

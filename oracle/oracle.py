@@ -194,6 +194,41 @@ def max_threads() -> int:
     return lib().tws_oracle_max_threads()
 
 
+def surface(b, d, v):
+    """The renderer's per-texel arithmetic (see tws_oracle_surface)."""
+    H, W = b.shape
+    out = {"height": np.empty((H, W), np.float32), "render_height": np.empty((H, W), np.float32),
+           "normal": np.empty((H, W, 3), np.float32), "flow_speed": np.empty((H, W), np.float32),
+           "foam": np.empty((H, W), np.float32), "dry": np.empty((H, W), np.uint8)}
+    L = lib()
+    L.tws_oracle_surface.argtypes = [C.c_int, C.c_int] + [C.c_void_p] * 9
+    b, d, v = (np.ascontiguousarray(a, dtype=np.float32) for a in (b, d, v))
+    L.tws_oracle_surface(W, H, _fp(b), _fp(d), _fp(v), *[_fp(out[k]) for k in
+                         ("height", "render_height", "normal", "flow_speed", "foam", "dry")])
+    return out
+
+
+def terrain_mips(b, d, levels):
+    """(RGBA32F TerrainData, [mip level 1..levels]) as the reference lays them out."""
+    H, W = b.shape
+    sizes, w, h = [], W, H
+    for _ in range(levels):
+        w, h = w // 2, h // 2
+        sizes.append((h, w))
+    rgba = np.empty((H, W, 4), np.float32)
+    mips = np.empty(max(1, sum(4 * hh * ww for hh, ww in sizes)), np.float32)
+    L = lib()
+    L.tws_oracle_terrain_mips.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                          C.c_void_p, C.c_void_p]
+    b, d = (np.ascontiguousarray(a, dtype=np.float32) for a in (b, d))
+    L.tws_oracle_terrain_mips(W, H, _fp(b), _fp(d), levels, _fp(rgba), _fp(mips))
+    out, off = [], 0
+    for hh, ww in sizes:
+        out.append(mips[off:off + 4 * hh * ww].reshape(hh, ww, 4))
+        off += 4 * hh * ww
+    return rgba, out
+
+
 # --------------------------------------------------------------------------- reference run
 
 def ref_steps(b, d, f, kf, ka, c, nsteps, brush=None):

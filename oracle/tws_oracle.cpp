@@ -423,6 +423,84 @@ double tws_oracle_volume_f64(const double* d, long long n, double cell_area) {
   return s * cell_area;
 }
 
+// ---------------------------------------------------------------------------
+// What the renderer reads (the water shaders' per-texel arithmetic), on
+// tightly packed W x H arrays; v holds 2 floats per cell.
+//   height = d + b                                  waterRender.vert:23
+//   dry = d < 0.1                                   waterRender.vert:22
+//   render_height = (d + b) - 0.1, minus 10 if dry  waterRender.eval:33-35
+//   normal = normalize(cross((0, h1-h0, 1), (1, h2-h3, 0))) with the four
+//            neighbours wrapping around (REPEAT sampler)  waterRender.frag:50-62
+//   flow = RG16F(v); speed = sqrt(dot(flow, flow));
+//   foam = saturate(dot(flow, flow) * 0.00004)      waterRender.frag:240-241, 341, 346
+// normalize is v / sqrt(dot(v, v)); the flow map rounds to nearest half.
+void tws_oracle_surface(int W, int H, const float* b, const float* d, const float* v,
+                        float* height, float* render_height, float* normal, float* speed,
+                        float* foam, unsigned char* dry) {
+  auto h = [&](int x, int y) { return d[(size_t)y * W + x] + b[(size_t)y * W + x]; };
+#pragma omp parallel for schedule(static)
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      const size_t i = (size_t)y * W + x;
+      const float hc = h(x, y);
+      if (height) height[i] = hc;
+      if (dry) dry[i] = d[i] < 0.1f ? 1 : 0;
+      if (render_height) {
+        float t = hc - 0.1f;
+        if (d[i] < 0.1f) t = t - 10.0f;
+        render_height[i] = t;
+      }
+      if (normal) {
+        const int xm = x == 0 ? W - 1 : x - 1, xp = x + 1 == W ? 0 : x + 1;
+        const int ym = y == 0 ? H - 1 : y - 1, yp = y + 1 == H ? 0 : y + 1;
+        const float A = h(x, yp) - h(x, ym), B = h(xp, y) - h(xm, y);
+        const float nx = -B, ny = 1.0f, nz = -A;
+        const float len = std::sqrt((nx * nx + ny * ny) + nz * nz);
+        normal[3 * i + 0] = nx / len;
+        normal[3 * i + 1] = ny / len;
+        normal[3 * i + 2] = nz / len;
+      }
+      if (speed || foam) {
+        const float fx = (float)(_Float16)v[2 * i], fy = (float)(_Float16)v[2 * i + 1];
+        const float s2 = fx * fx + fy * fy;
+        if (speed) speed[i] = std::sqrt(s2);
+        if (foam) foam[i] = glsl_saturate(s2 * 0.00004f);
+      }
+    }
+}
+
+// TerrainData as RGBA32F (r = b, g = b = 0.3, a = d; Terrain.cpp:216-220), then
+// `levels` 2x2 box-filtered mip levels, each ((t00 + t10) + (t01 + t11)) * 0.25
+// per channel, packed level after level in `mips`.
+void tws_oracle_terrain_mips(int W, int H, const float* b, const float* d, int levels,
+                             float* rgba, float* mips) {
+  for (size_t i = 0; i < (size_t)W * H; ++i) {
+    rgba[4 * i + 0] = b[i];
+    rgba[4 * i + 1] = 0.3f;
+    rgba[4 * i + 2] = 0.3f;
+    rgba[4 * i + 3] = d[i];
+  }
+  const float* src = rgba;
+  float* dst = mips;
+  int sw = W, sh = H;
+  for (int l = 1; l <= levels; ++l) {
+    const int dw = sw / 2, dh = sh / 2;
+    for (int y = 0; y < dh; ++y)
+      for (int x = 0; x < dw; ++x)
+        for (int c = 0; c < 4; ++c) {
+          const float t00 = src[4 * ((size_t)(2 * y) * sw + 2 * x) + c];
+          const float t10 = src[4 * ((size_t)(2 * y) * sw + 2 * x + 1) + c];
+          const float t01 = src[4 * ((size_t)(2 * y + 1) * sw + 2 * x) + c];
+          const float t11 = src[4 * ((size_t)(2 * y + 1) * sw + 2 * x + 1) + c];
+          dst[4 * ((size_t)y * dw + x) + c] = ((t00 + t10) + (t01 + t11)) * 0.25f;
+        }
+    src = dst;
+    dst += 4 * (size_t)dw * dh;
+    sw = dw;
+    sh = dh;
+  }
+}
+
 int tws_oracle_max_threads(void) { return num_threads(0); }
 
 }  // extern "C"

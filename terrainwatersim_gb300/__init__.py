@@ -73,6 +73,11 @@ class Source(C.Structure):
                 ("radius", C.c_float), ("rate", C.c_float)]
 
 
+class SurfaceOut(C.Structure):
+    _fields_ = [("height", C.c_void_p), ("render_height", C.c_void_p), ("normal", C.c_void_p),
+                ("flow_speed", C.c_void_p), ("foam", C.c_void_p), ("dry", C.c_void_p)]
+
+
 class Buffers(C.Structure):
     _fields_ = [("terrain", C.c_void_p), ("depth", C.c_void_p), ("flux", C.c_void_p),
                 ("velocity", C.c_void_p), ("width", C.c_int), ("height", C.c_int),
@@ -138,6 +143,8 @@ def _declare(L):
         "tws_server_result": ([vp, i, vp], i),
         "tws_server_stats": ([vp, vp, vp, vp, vp], i),
         "tws_grid_bytes": ([i, i, i], d),
+        "tws_surface": ([vp, vp], i),
+        "tws_export_textures": ([vp, vp, vp, i, vp], i),
         "tws_version": ([], C.c_char_p),
     }
     for name, (args, res) in sig.items():
@@ -319,6 +326,16 @@ class Grid:
                                   f.ctypes.data if f is not None else None,
                                   v.ctypes.data if v is not None else None), self._h)
         return d, f, v
+
+    def surface(self, out: "SurfaceOut"):
+        """The renderer's per-texel outputs into caller-owned device buffers."""
+        _check(lib().tws_surface(self._h, C.byref(out)), self._h)
+
+    def export_textures(self, terrain_rgba_ptr, flowmap_ptr, mip_levels=0, mips_ptr=None):
+        """The reference's RGBA32F TerrainData (+ mips) and RG16F FlowMap into
+        caller-owned device buffers."""
+        _check(lib().tws_export_textures(self._h, terrain_rgba_ptr, flowmap_ptr, mip_levels,
+                                         mips_ptr), self._h)
 
     def download_terrain(self):
         b = np.empty((self.height, self.width), np.float32)

@@ -48,11 +48,12 @@ struct tws_grid {
   std::vector<VariantMaps> maps;
   tws_source src[TWS_MAX_SOURCES];
   int nsrc = 0;
+  char* slab = nullptr;  // the one device allocation holding everything below
   double* vol_partials = nullptr;
   double* vol_out = nullptr;
-  double* vol_host = nullptr;  // pinned
-  int* err = nullptr;          // device error word
-  int* err_host = nullptr;     // pinned
+  double vol_host[1] = {0.0};
+  int* err = nullptr;     // device error word
+  int err_host[1] = {0};
   tws_batch* batch = nullptr;  // batch this grid belongs to (its stream is the batch's)
   cudaStream_t home_stream = nullptr;
   std::string last_error;
@@ -77,6 +78,31 @@ int cuda_fail(tws_grid* g, cudaError_t e, const char* what) {
   } while (0)
 
 size_t flux_bytes_per_cell(int storage) { return storage == TWS_FLUX_F16 ? 8 : 16; }
+
+// The library's own stream-ordered memory pool per device.  Freed memory
+// stays in the pool (release threshold: never) so that grids created after
+// others were destroyed reuse it without going back to the driver.
+cudaMemPool_t library_pool(int device) {
+  static std::mutex mu;
+  static cudaMemPool_t pools[64] = {};
+  if (device < 0 || device >= 64) return nullptr;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!pools[device]) {
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    cudaMemPool_t p = nullptr;
+    if (cudaMemPoolCreate(&p, &props) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+    pools[device] = p;
+  }
+  return pools[device];
+}
 
 bool params_ok(const tws_sim_params* p) {
   if (!p) return false;
@@ -296,20 +322,34 @@ TWS_API int tws_create(int width, int height, const tws_sim_params* params, int 
   }
   const size_t n = (size_t)g->pitch * g->H;
   const size_t fb = flux_bytes_per_cell(flux_storage);
-  if (cudaMalloc(&g->b, n * 4) != cudaSuccess || cudaMalloc(&g->d[0], n * 4) != cudaSuccess ||
-      cudaMalloc(&g->d[1], n * 4) != cudaSuccess || cudaMalloc(&g->f[0], n * fb) != cudaSuccess ||
-      cudaMalloc(&g->f[1], n * fb) != cudaSuccess || cudaMalloc(&g->v, n * 8) != cudaSuccess ||
-      cudaMalloc(&g->vol_partials, sizeof(double) * volume_partials_needed()) != cudaSuccess ||
-      cudaMalloc(&g->vol_out, sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&g->err, sizeof(int)) != cudaSuccess) {
+  // All device state in one stream-ordered allocation from the library's
+  // pool: creating and destroying grids (the serving loop does it per
+  // request) never synchronises the device.
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off += (bytes + 255) / 256 * 256;
+    return o;
+  };
+  const size_t ob = take(n * 4), od0 = take(n * 4), od1 = take(n * 4), of0 = take(n * fb),
+               of1 = take(n * fb), ov = take(n * 8),
+               op = take(sizeof(double) * volume_partials_needed()), oo = take(sizeof(double)),
+               oe = take(sizeof(int));
+  cudaMemPool_t pool = library_pool(g->device);
+  if (!pool || cudaMallocFromPoolAsync(reinterpret_cast<void**>(&g->slab), off, pool, g->stream) !=
+                   cudaSuccess) {
     cudaGetLastError();
     return bail(TWS_ERR_OOM);
   }
-  if (cudaMallocHost(&g->vol_host, sizeof(double)) != cudaSuccess ||
-      cudaMallocHost(&g->err_host, sizeof(int)) != cudaSuccess) {
-    cudaGetLastError();
-    return bail(TWS_ERR_OOM);
-  }
+  g->b = reinterpret_cast<float*>(g->slab + ob);
+  g->d[0] = reinterpret_cast<float*>(g->slab + od0);
+  g->d[1] = reinterpret_cast<float*>(g->slab + od1);
+  g->f[0] = g->slab + of0;
+  g->f[1] = g->slab + of1;
+  g->v = reinterpret_cast<float2*>(g->slab + ov);
+  g->vol_partials = reinterpret_cast<double*>(g->slab + op);
+  g->vol_out = reinterpret_cast<double*>(g->slab + oo);
+  g->err = reinterpret_cast<int*>(g->slab + oe);
   // Zero everything, padding included (the F16 flux map reads the padding
   // cell of odd-width rows and relies on it staying zero).
   cudaMemsetAsync(g->b, 0, n * 4, g->stream);
@@ -327,18 +367,9 @@ TWS_API int tws_create(int width, int height, const tws_sim_params* params, int 
 TWS_API int tws_destroy(tws_grid* g) {
   if (!g) return TWS_ERR_INVALID;
   if (g->batch) tws_batch_remove(g->batch, g);
-  if (g->stream) cudaStreamSynchronize(g->stream);
-  cudaFree(g->b);
-  cudaFree(g->d[0]);
-  cudaFree(g->d[1]);
-  cudaFree(g->f[0]);
-  cudaFree(g->f[1]);
-  cudaFree(g->v);
-  cudaFree(g->vol_partials);
-  cudaFree(g->vol_out);
-  cudaFree(g->err);
-  if (g->vol_host) cudaFreeHost(g->vol_host);
-  if (g->err_host) cudaFreeHost(g->err_host);
+  // stream-ordered: the memory returns to the pool once the grid's queued
+  // work is done, without waiting here
+  if (g->slab) cudaFreeAsync(g->slab, g->stream);
   if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
   delete g;
   return TWS_OK;
@@ -584,6 +615,30 @@ TWS_API int tws_download_terrain(tws_grid* g, float* b) {
   return TWS_OK;
 }
 
+TWS_API int tws_surface(tws_grid* g, const tws_surface_out* o) {
+  if (!g || !o) return fail(g, TWS_ERR_INVALID, "null surface output");
+  TWS_CUDA(g, launch_surface(g->b, g->d[g->cur], g->v, g->W, g->H, g->pitch, *o, g->stream),
+           "surface kernel");
+  return TWS_OK;
+}
+
+TWS_API int tws_export_textures(tws_grid* g, float* terrain_rgba, uint16_t* flowmap,
+                                int mip_levels, float* mips) {
+  if (!g || mip_levels < 0) return fail(g, TWS_ERR_INVALID, "bad export arguments");
+  if (mip_levels > 0 && (!terrain_rgba || !mips))
+    return fail(g, TWS_ERR_INVALID, "mips need terrain_rgba and mips buffers");
+  int w = g->W, h = g->H;
+  for (int l = 1; l <= mip_levels; ++l) {
+    if (w < 2 || h < 2) return fail(g, TWS_ERR_INVALID, "mip level smaller than 1x1");
+    w /= 2;
+    h /= 2;
+  }
+  TWS_CUDA(g, launch_export(g->b, g->d[g->cur], g->v, g->W, g->H, g->pitch, terrain_rgba, flowmap,
+                            mip_levels, mips, g->stream),
+           "export kernels");
+  return TWS_OK;
+}
+
 TWS_API int tws_get_buffers(tws_grid* g, tws_buffers* out) {
   if (!g || !out) return TWS_ERR_INVALID;
   out->terrain = g->b;
@@ -650,6 +705,8 @@ struct tws_batch {
   };
   std::vector<Graph> graphs;
   uint64_t chains = 0, graph_launches = 0;
+  int* d_err = nullptr;  // one device error word for every member while batched
+  int h_err = 0;
   std::string last_error;
 };
 
@@ -773,6 +830,7 @@ int run_chain(tws_batch* b, int variant, const std::vector<int>& launches) {
     e.tm_f[0] = maps->f[0];
     e.tm_f[1] = maps->f[1];
     e.a = make_step_args(g);
+    e.a.err = b->d_err;
     e.d[0] = g->d[0];
     e.d[1] = g->d[1];
     e.f[0] = g->f[0];
@@ -867,6 +925,14 @@ TWS_API int tws_batch_create(int flux_storage, void* stream, tws_batch** out) {
     }
     b->own_stream = true;
   }
+  if (cudaMalloc(&b->d_err, sizeof(int)) != cudaSuccess ||
+      cudaMemsetAsync(b->d_err, 0, sizeof(int), b->stream) != cudaSuccess) {
+    cudaGetLastError();
+    if (b->own_stream) cudaStreamDestroy(b->stream);
+    cudaFree(b->d_err);
+    delete b;
+    return TWS_ERR_CUDA;
+  }
   *out = b;
   return TWS_OK;
 }
@@ -888,6 +954,7 @@ TWS_API int tws_batch_destroy(tws_batch* b) {
   free_table(b);
   for (int s = 0; s < 2; ++s)
     if (b->copied[s]) cudaEventDestroy(b->copied[s]);
+  cudaFree(b->d_err);
   if (b->own_stream) cudaStreamDestroy(b->stream);
   delete b;
   return TWS_OK;
@@ -1019,11 +1086,12 @@ TWS_API int tws_batch_autotune(tws_batch* b, int trial_steps, int* chosen) {
 
 TWS_API int tws_batch_sync(tws_batch* b) {
   if (!b) return TWS_ERR_INVALID;
-  if (cudaStreamSynchronize(b->stream) != cudaSuccess) return bfail(b, TWS_ERR_CUDA, "batch sync");
-  for (tws_grid* g : b->grids) {
-    const int rc = tws_sync(g);
-    if (rc != TWS_OK) return bfail(b, rc, g->last_error);
-  }
+  if (cudaMemcpyAsync(&b->h_err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost, b->stream) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(b->stream) != cudaSuccess)
+    return bfail(b, TWS_ERR_CUDA, "batch sync");
+  if (b->h_err != kDevErrNone)
+    return bfail(b, TWS_ERR_TIMEOUT, "a batched kernel gave up waiting for its tile loads");
   return TWS_OK;
 }
 

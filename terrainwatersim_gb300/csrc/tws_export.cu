@@ -1,0 +1,148 @@
+// tws_export.cu -- what the renderer reads from the simulation, on the device.
+//
+// * surface_kernel: the water shaders' per-texel arithmetic on the step's
+//   outputs, written to plain device buffers (no graphics API):
+//     surface height d + b                     waterRender.vert:23
+//     dry mask d < 0.1                         waterRender.vert:22
+//     tessellated height (d + b) - 0.1, and 10 lower where dry
+//                                              waterRender.eval:33-35
+//     heightmap normal from the 4 neighbour surface heights, sampled through
+//     a REPEAT sampler (Terrain.cpp:313, 112-113)  waterRender.frag:50-62
+//     flow speed |flow| and foam blend saturate(|flow|^2 * 0.00004) from the
+//     RG16F flow map                           waterRender.frag:217,240-241,341,346
+// * export kernels: the reference's texture layouts -- TerrainData as RGBA32F
+//   (.r terrain, .g .b 0.3, .a depth; Terrain.cpp:216-220) with the 2x2 box
+//   mip pyramid glGenerateMipmap builds after the steps (Terrain.cpp:273-276),
+//   and the FlowMap as RG16F (flowApply.comp:7).
+// Arithmetic is IEEE round-to-nearest without contraction; `normalize` is
+// v / sqrt(dot(v, v)) and the mip filter ((a + b) + (c + d)) * 0.25 per
+// channel (the GL specification leaves both to the implementation).
+
+#include "tws_device.cuh"
+#include "tws_internal.h"
+
+namespace tws {
+namespace {
+
+__device__ __forceinline__ float surf(const float* b, const float* d, size_t i) {
+  return fadd(d[i], b[i]);
+}
+
+__device__ __forceinline__ float half_round(float v) { return __half2float(__float2half_rn(v)); }
+
+__global__ void surface_kernel(const float* __restrict__ b, const float* __restrict__ d,
+                               const float2* __restrict__ v, int W, int H, int pitch,
+                               tws_surface_out o) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= W || y >= H) return;
+  const size_t i = (size_t)y * pitch + x;
+  const size_t out = (size_t)y * W + x;
+  const float dc = d[i];
+  const float h = surf(b, d, i);
+  if (o.height) o.height[out] = h;
+  if (o.dry) o.dry[out] = dc < 0.1f ? 1 : 0;
+  if (o.render_height) {
+    float t = fsub(h, 0.1f);
+    if (dc < 0.1f) t = fsub(t, 10.0f);
+    o.render_height[out] = t;
+  }
+  if (o.normal) {
+    const int xm = x == 0 ? W - 1 : x - 1, xp = x + 1 == W ? 0 : x + 1;
+    const int ym = y == 0 ? H - 1 : y - 1, yp = y + 1 == H ? 0 : y + 1;
+    const float h0 = surf(b, d, (size_t)ym * pitch + x);
+    const float h1 = surf(b, d, (size_t)yp * pitch + x);
+    const float h2 = surf(b, d, (size_t)y * pitch + xp);
+    const float h3 = surf(b, d, (size_t)y * pitch + xm);
+    const float A = fsub(h1, h0), B = fsub(h2, h3);
+    // cross((0, A, 1), (1, B, 0)) = (-B, 1, -A)
+    const float nx = -B, ny = 1.0f, nz = -A;
+    const float len = __fsqrt_rn(fadd(fadd(fmul(nx, nx), fmul(ny, ny)), fmul(nz, nz)));
+    o.normal[3 * out + 0] = fdiv(nx, len);
+    o.normal[3 * out + 1] = fdiv(ny, len);
+    o.normal[3 * out + 2] = fdiv(nz, len);
+  }
+  if (o.flow_speed || o.foam) {
+    const float2 fv = v[i];
+    const float fx = half_round(fv.x), fy = half_round(fv.y);
+    const float s2 = fadd(fmul(fx, fx), fmul(fy, fy));
+    if (o.flow_speed) o.flow_speed[out] = __fsqrt_rn(s2);
+    if (o.foam) o.foam[out] = saturate01(fmul(s2, 0.00004f));
+  }
+}
+
+__global__ void terrain_rgba_kernel(const float* __restrict__ b, const float* __restrict__ d,
+                                    int W, int H, int pitch, float4* __restrict__ out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= W || y >= H) return;
+  const size_t i = (size_t)y * pitch + x;
+  out[(size_t)y * W + x] = make_float4(b[i], 0.3f, 0.3f, d[i]);
+}
+
+__global__ void flowmap_kernel(const float2* __restrict__ v, int W, int H, int pitch,
+                               __half2* __restrict__ out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= W || y >= H) return;
+  const float2 fv = v[(size_t)y * pitch + x];
+  out[(size_t)y * W + x] = __floats2half2_rn(fv.x, fv.y);
+}
+
+__device__ __forceinline__ float avg4(float a, float b, float c, float d) {
+  return fmul(fadd(fadd(a, b), fadd(c, d)), 0.25f);
+}
+
+__global__ void mip_kernel(const float4* __restrict__ src, int sw, float4* __restrict__ dst,
+                           int dw, int dh) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= dw || y >= dh) return;
+  const float4 a = src[(size_t)(2 * y) * sw + 2 * x], b = src[(size_t)(2 * y) * sw + 2 * x + 1];
+  const float4 c = src[(size_t)(2 * y + 1) * sw + 2 * x],
+               e = src[(size_t)(2 * y + 1) * sw + 2 * x + 1];
+  dst[(size_t)y * dw + x] = make_float4(avg4(a.x, b.x, c.x, e.x), avg4(a.y, b.y, c.y, e.y),
+                                        avg4(a.z, b.z, c.z, e.z), avg4(a.w, b.w, c.w, e.w));
+}
+
+dim3 grid2d(int w, int h) { return dim3((w + 31) / 32, (h + 7) / 8); }
+
+}  // namespace
+
+cudaError_t launch_surface(const float* b, const float* d, const float2* v, int W, int H,
+                           int pitch, const tws_surface_out& o, cudaStream_t s) {
+  surface_kernel<<<grid2d(W, H), dim3(32, 8), 0, s>>>(b, d, v, W, H, pitch, o);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_export(const float* b, const float* d, const float2* v, int W, int H,
+                          int pitch, float* terrain_rgba, uint16_t* flowmap, int mip_levels,
+                          float* mips, cudaStream_t s) {
+  if (flowmap) {
+    flowmap_kernel<<<grid2d(W, H), dim3(32, 8), 0, s>>>(v, W, H, pitch,
+                                                         reinterpret_cast<__half2*>(flowmap));
+    count_launch();
+  }
+  if (terrain_rgba) {
+    terrain_rgba_kernel<<<grid2d(W, H), dim3(32, 8), 0, s>>>(b, d, W, H, pitch,
+                                                              reinterpret_cast<float4*>(terrain_rgba));
+    count_launch();
+    const float4* src = reinterpret_cast<const float4*>(terrain_rgba);
+    float4* dst = reinterpret_cast<float4*>(mips);
+    int sw = W, sh = H;
+    for (int l = 1; l <= mip_levels && mips; ++l) {
+      const int dw = sw / 2 > 0 ? sw / 2 : 1, dh = sh / 2 > 0 ? sh / 2 : 1;
+      if (sw < 2 || sh < 2) break;
+      mip_kernel<<<grid2d(dw, dh), dim3(32, 8), 0, s>>>(src, sw, dst, dw, dh);
+      count_launch();
+      src = dst;
+      dst += (size_t)dw * dh;
+      sw = dw;
+      sh = dh;
+    }
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace tws

@@ -110,6 +110,13 @@ cudaError_t launch_flux_to_f32(const void* f, int flux_storage, float inv_scale,
 cudaError_t launch_flux_from_f32(const float* in_packed, int flux_storage, float scale, int W,
                                  int H, int pitch, void* f, cudaStream_t st);
 
+// tws_export.cu
+cudaError_t launch_surface(const float* b, const float* d, const float2* v, int W, int H,
+                           int pitch, const tws_surface_out& o, cudaStream_t s);
+cudaError_t launch_export(const float* b, const float* d, const float2* v, int W, int H,
+                          int pitch, float* terrain_rgba, uint16_t* flowmap, int mip_levels,
+                          float* mips, cudaStream_t s);
+
 DevSource make_dev_source(const tws_source& s);
 void count_launch(uint64_t n = 1);
 

@@ -29,6 +29,10 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
+// Work per chain when chains are sized automatically: about 15 ms at
+// 100 G cell-steps/s.
+constexpr double kChainCellSteps = 1.5e9;
+
 struct Admitted {
   tws_request req;
   tws_grid* grid = nullptr;
@@ -120,7 +124,7 @@ void wait_for_work(tws_server* s, Clock::time_point t0, double next_arrival) {
 
 int run_batched(tws_server* s) {
   const tws_server_config& cfg = s->cfg;
-  const int chain = cfg.chain_steps > 0 ? cfg.chain_steps : 16;
+  const int chain = cfg.chain_steps > 0 ? cfg.chain_steps : 16;  // fixed chain length
   tws_batch* batch = nullptr;
   int rc = tws_batch_create(cfg.flux_storage, nullptr, &batch);
   if (rc != TWS_OK) return rc;
@@ -210,8 +214,18 @@ int run_batched(tws_server* s) {
       tws_batch_autotune(batch, 16, &v);
       tuned = true;
     }
+    // Steps this chain: fixed, or (chain_steps <= 0) sized so a chain is about
+    // kChainCellSteps cell-steps of work -- long enough that the host work
+    // between chains is small, short enough that new arrivals join soon.
+    int this_chain = chain;
+    if (cfg.chain_steps <= 0) {
+      double cells = 0.0;
+      for (const Admitted& a : active) cells += (double)a.req.width * a.req.height;
+      const double want = kChainCellSteps / std::max(1.0, cells);
+      this_chain = std::max(16, std::min(512, (int)(want / 16.0) * 16));
+    }
     std::vector<int> steps(active.size());
-    for (size_t i = 0; i < active.size(); ++i) steps[i] = std::min(active[i].left, chain);
+    for (size_t i = 0; i < active.size(); ++i) steps[i] = std::min(active[i].left, this_chain);
     rc = tws_batch_step_each(batch, steps.data(), (int)steps.size());
     if (rc != TWS_OK) break;
     ++s->chains;

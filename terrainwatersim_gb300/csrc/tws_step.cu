@@ -163,14 +163,21 @@ __device__ __forceinline__ void issue_tile(unsigned char* st, uint64_t* bar,
 }
 
 // K steps of one tile whose loads have landed in (sb, sd, sf-or-staging).
-template <int K, int TX, int TY, bool F16, int STAGES>
+// INTERIOR: the tile's whole b/d box lies inside the grid, so no cell it
+// computes is off the grid or on the border (no bounds or wall checks).
+template <int K, int TX, int TY, bool F16, int STAGES, bool INTERIOR>
 __device__ __forceinline__ void process_tile(const StepArgs& a, float* __restrict__ d_out,
                                              void* __restrict__ f_out, float2* __restrict__ v_out,
                                              int x0, int y0, uint32_t mask, float* sb, float* sd,
                                              float* sh, float4* sf, const unsigned char* staging) {
   using T = Tile<K, TX, TY, F16, STAGES>;
   const int tid = threadIdx.x;
+  // The per-grid scalars, read once (in the batched kernel `a` lives in
+  // global memory; in registers the loops below do not reload them).
   const int W = a.W, H = a.H;
+  const float kf = a.kf, ka = a.ka, cc = a.c;
+  const float fscale = a.flux_scale, finv = a.flux_inv_scale;
+  const bool closed = a.closed != 0;
 
   // Phase 0: first step's sources, surface height h = d + b (flowUpdate.comp:34).
   for (int idx = tid; idx < T::NB; idx += kThreads) {
@@ -178,7 +185,7 @@ __device__ __forceinline__ void process_tile(const StepArgs& a, float* __restric
     if (mask) {
       const int i = idx / T::BW, j = idx - (idx / T::BW) * T::BW;
       const int gx = x0 - T::HX + j, gy = y0 - T::HY + i;
-      if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+      if (INTERIOR || (gx >= 0 && gx < W && gy >= 0 && gy < H)) {
         d = add_sources(d, gx, gy, a, mask);
         sd[idx] = d;
       }
@@ -191,8 +198,8 @@ __device__ __forceinline__ void process_tile(const StepArgs& a, float* __restric
       const int i = idx / T::FW, j = idx - (idx / T::FW) * T::FW;
       const int s = i * T::SW + j + 1;
       const float2 lo = __half22float2(st[2 * s]), hi = __half22float2(st[2 * s + 1]);
-      sf[idx] = make_float4(fmul(lo.x, a.flux_inv_scale), fmul(lo.y, a.flux_inv_scale),
-                            fmul(hi.x, a.flux_inv_scale), fmul(hi.y, a.flux_inv_scale));
+      sf[idx] = make_float4(fmul(lo.x, finv), fmul(lo.y, finv), fmul(hi.x, finv),
+                            fmul(hi.y, finv));
     }
   }
   __syncthreads();
@@ -209,7 +216,7 @@ __device__ __forceinline__ void process_tile(const StepArgs& a, float* __restric
         const int i = idx / RW, j = idx - (idx / RW) * RW;
         const int fi = T::RF - rf + i, fj = T::RF - rf + j;
         const int gx = x0 - T::RF + fj, gy = y0 - T::RF + fi;
-        if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
+        if (!INTERIOR && (gx < 0 || gx >= W || gy < 0 || gy >= H)) continue;
         const int bidx = (fi + T::HY - T::RF) * T::BW + (fj + T::HX - T::RF);
         const float hc = sh[bidx];
         const float ex1 = fsub(hc, sh[bidx + 1]);
@@ -220,17 +227,17 @@ __device__ __forceinline__ void process_tile(const StepArgs& a, float* __restric
         const int fidx = fi * T::FW + fj;
         const float4 fo = sf[fidx];
         float4 nf;
-        nf.x = max0(fadd(fmul(fo.x, a.kf), fmul(ex1, a.ka)));
-        nf.y = max0(fadd(fmul(fo.y, a.kf), fmul(ex0, a.ka)));
-        nf.z = max0(fadd(fmul(fo.z, a.kf), fmul(ey1, a.ka)));
-        nf.w = max0(fadd(fmul(fo.w, a.kf), fmul(ey0, a.ka)));
-        if (a.closed) {
+        nf.x = max0(fadd(fmul(fo.x, kf), fmul(ex1, ka)));
+        nf.y = max0(fadd(fmul(fo.y, kf), fmul(ex0, ka)));
+        nf.z = max0(fadd(fmul(fo.z, kf), fmul(ey1, ka)));
+        nf.w = max0(fadd(fmul(fo.w, kf), fmul(ey0, ka)));
+        if (!INTERIOR && closed) {
           if (gx + 1 >= W) nf.x = 0.0f;
           if (gx == 0) nf.y = 0.0f;
           if (gy + 1 >= H) nf.z = 0.0f;
           if (gy == 0) nf.w = 0.0f;
         }
-        const float total = fmul(fadd(fadd(fadd(nf.x, nf.y), nf.z), nf.w), a.c);
+        const float total = fmul(fadd(fadd(fadd(nf.x, nf.y), nf.z), nf.w), cc);
         if (total > dc) {
           const float sc = fdiv(dc, total);
           nf.x = fmul(nf.x, sc);
@@ -239,10 +246,10 @@ __device__ __forceinline__ void process_tile(const StepArgs& a, float* __restric
           nf.w = fmul(nf.w, sc);
         }
         if (F16) {
-          nf.x = quantize_f16(nf.x, a.flux_scale, a.flux_inv_scale);
-          nf.y = quantize_f16(nf.y, a.flux_scale, a.flux_inv_scale);
-          nf.z = quantize_f16(nf.z, a.flux_scale, a.flux_inv_scale);
-          nf.w = quantize_f16(nf.w, a.flux_scale, a.flux_inv_scale);
+          nf.x = quantize_f16(nf.x, fscale, finv);
+          nf.y = quantize_f16(nf.y, fscale, finv);
+          nf.z = quantize_f16(nf.z, fscale, finv);
+          nf.w = quantize_f16(nf.w, fscale, finv);
         }
         sf[fidx] = nf;
       }
@@ -256,7 +263,7 @@ __device__ __forceinline__ void process_tile(const StepArgs& a, float* __restric
         const int i = idx / RW, j = idx - (idx / RW) * RW;
         const int fi = T::RF - rd + i, fj = T::RF - rd + j;
         const int gx = x0 - T::RF + fj, gy = y0 - T::RF + fi;
-        if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
+        if (!INTERIOR && (gx < 0 || gx >= W || gy < 0 || gy >= H)) continue;
         const int fidx = fi * T::FW + fj;
         const float4 fc = sf[fidx];
         const float X1 = sf[fidx + 1].y;      // -x outflow of the +x neighbour
@@ -266,15 +273,15 @@ __device__ __forceinline__ void process_tile(const StepArgs& a, float* __restric
         const int bidx = (fi + T::HY - T::RF) * T::BW + (fj + T::HX - T::RF);
         const float in = fadd(fadd(fadd(X1, X0), Y1), Y0);
         const float out = fadd(fadd(fadd(fc.x, fc.y), fc.z), fc.w);
-        const float dn = max0(fadd(sd[bidx], fmul(fsub(in, out), a.c)));
+        const float dn = max0(fadd(sd[bidx], fmul(fsub(in, out), cc)));
         if (s == K - 1) {
           const size_t g = (size_t)gy * a.pitch + gx;
           d_out[g] = dn;
           if (F16) {
             const __half2 lo =
-                __floats2half2_rn(fmul(fc.x, a.flux_scale), fmul(fc.y, a.flux_scale));
+                __floats2half2_rn(fmul(fc.x, fscale), fmul(fc.y, fscale));
             const __half2 hi =
-                __floats2half2_rn(fmul(fc.z, a.flux_scale), fmul(fc.w, a.flux_scale));
+                __floats2half2_rn(fmul(fc.z, fscale), fmul(fc.w, fscale));
             uint2 packed;
             packed.x = *reinterpret_cast<const uint32_t*>(&lo);
             packed.y = *reinterpret_cast<const uint32_t*>(&hi);
@@ -353,8 +360,12 @@ __global__ void __launch_bounds__(kThreads)
     const bool ok = wait_bounded(&bars[s], parity, a.err);
     if (__syncthreads_or(!ok)) return;  // every thread leaves together on a time-out
 
-    process_tile<K, TX, TY, F16, STAGES>(a, a.d_out, a.f_out, a.v_out, x0, y0, mask, sb, sd, sh,
-                                         sf, st + T::ST_F);
+    if (x0 - T::HX >= 0 && y0 - T::HY >= 0 && x0 + TX + T::HX <= a.W && y0 + TY + T::HY <= a.H)
+      process_tile<K, TX, TY, F16, STAGES, true>(a, a.d_out, a.f_out, a.v_out, x0, y0, mask, sb,
+                                                 sd, sh, sf, st + T::ST_F);
+    else
+      process_tile<K, TX, TY, F16, STAGES, false>(a, a.d_out, a.f_out, a.v_out, x0, y0, mask, sb,
+                                                  sd, sh, sf, st + T::ST_F);
     __syncthreads();  // stage s, h and the F16 working copy are free again
 
     if (tid == 0) {
@@ -384,7 +395,7 @@ __device__ __forceinline__ void tensormap_acquire(const void* tm) {
 // step_kernel.  Launch `launch_idx` of a chain skips grids that have taken
 // all their launches, so grids with different step counts share a chain.
 template <int K, int TX, int TY, bool F16>
-__global__ void __launch_bounds__(kThreads, 6)
+__global__ void __launch_bounds__(kThreads, 5)
     batch_kernel(const BatchGrid* __restrict__ grids, const int* __restrict__ unit_base,
                  const int* __restrict__ hdr, int launch_idx) {
   using T = Tile<K, TX, TY, F16, 1>;
@@ -441,8 +452,13 @@ __global__ void __launch_bounds__(kThreads, 6)
     const bool ok = wait_bounded(bar, it & 1u, a.err);
     ++it;
     if (__syncthreads_or(!ok)) return;
-    process_tile<K, TX, TY, F16, 1>(a, G.d[p ^ 1], G.f[p ^ 1], G.v, x0, y0, mask, sb, sd, sh, sf,
-                                    smem + T::ST_F);
+    const int gw = a.W, gh = a.H;
+    if (x0 - T::HX >= 0 && y0 - T::HY >= 0 && x0 + TX + T::HX <= gw && y0 + TY + T::HY <= gh)
+      process_tile<K, TX, TY, F16, 1, true>(a, G.d[p ^ 1], G.f[p ^ 1], G.v, x0, y0, mask, sb, sd,
+                                            sh, sf, smem + T::ST_F);
+    else
+      process_tile<K, TX, TY, F16, 1, false>(a, G.d[p ^ 1], G.f[p ^ 1], G.v, x0, y0, mask, sb, sd,
+                                             sh, sf, smem + T::ST_F);
     __syncthreads();  // the tile buffers are free again
   }
 }

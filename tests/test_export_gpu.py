@@ -1,0 +1,78 @@
+"""GPU tests of what the renderer reads: the water shaders' per-texel
+arithmetic (surface height, dry mask, tessellated height, heightmap normal,
+flow speed, foam) and the reference's texture layouts (RGBA32F TerrainData
+with its mip pyramid, RG16F FlowMap), bit for bit against the oracle."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import assert_bitexact
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def tws():
+    import terrainwatersim_gb300 as t
+    t.lib()
+    return t
+
+
+@pytest.mark.parametrize("W,H", [(96, 80), (33, 257), (1, 5)])
+def test_surface_outputs_match_oracle(tws, oracle, W, H):
+    import torch
+    p = tws.params_physical(boundary=tws.BOUNDARY_OPEN)
+    with tws.Grid(W, H, p) as g:
+        g.generate_scene(12, 40.0, 15.0)
+        g.apply_source((tws.SOURCE_BRUSH, W * 0.4, H * 0.3, 40.0, 6.0))
+        g.step(25)
+        d, _, v = g.download(flux=False)
+        b = g.download_terrain()
+        bufs = {k: torch.zeros((H, W), dtype=torch.float32, device="cuda")
+                for k in ("height", "render_height", "flow_speed", "foam")}
+        bufs["normal"] = torch.zeros((H, W, 3), dtype=torch.float32, device="cuda")
+        bufs["dry"] = torch.zeros((H, W), dtype=torch.uint8, device="cuda")
+        torch.cuda.synchronize()
+        out = tws.SurfaceOut(*[bufs[k].data_ptr() for k in
+                               ("height", "render_height", "normal", "flow_speed", "foam", "dry")])
+        g.surface(out)
+        g.sync()
+        got = {k: t.cpu().numpy() for k, t in bufs.items()}
+    want = oracle.surface(b, d, v)
+    for k in ("height", "render_height", "normal", "flow_speed", "foam"):
+        assert_bitexact(got[k], want[k], k)
+    assert np.array_equal(got["dry"], want["dry"])
+    assert got["dry"].any() and (got["flow_speed"] > 0).any()
+
+
+@pytest.mark.parametrize("W,H,levels", [(64, 48, 3), (100, 37, 2), (256, 256, 8)])
+def test_texture_export_matches_oracle(tws, oracle, W, H, levels):
+    import torch
+    with tws.Grid(W, H) as g:
+        g.generate_scene(4, 40.0, 15.0)
+        g.set_sources(tws.rain_disks(4, W, H, 5, 0.05, 1))
+        g.step(9)
+        d, _, v = g.download(flux=False)
+        b = g.download_terrain()
+        rgba = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+        fm = torch.zeros((H, W, 2), dtype=torch.int16, device="cuda")
+        n = 0
+        w, h = W, H
+        for _ in range(levels):
+            w, h = w // 2, h // 2
+            n += 4 * w * h
+        mips = torch.zeros(max(1, n), dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        g.export_textures(rgba.data_ptr(), fm.data_ptr(), levels, mips.data_ptr())
+        g.sync()
+        got_rgba, got_fm, got_mips = rgba.cpu().numpy(), fm.cpu().numpy(), mips.cpu().numpy()
+        with pytest.raises(tws.TwsError):
+            g.export_textures(rgba.data_ptr(), None, 20, mips.data_ptr())  # past 1x1
+    want_rgba, want_mips = oracle.terrain_mips(b, d, levels)
+    assert_bitexact(got_rgba, want_rgba, "TerrainData")
+    assert np.array_equal(got_fm.view(np.uint16), v.astype(np.float16).view(np.uint16))
+    off = 0
+    for lvl, m in enumerate(want_mips, 1):
+        assert_bitexact(got_mips[off:off + m.size].reshape(m.shape), m, f"mip {lvl}")
+        off += m.size

@@ -43,7 +43,8 @@ def test_surface_outputs_match_oracle(tws, oracle, W, H):
     for k in ("height", "render_height", "normal", "flow_speed", "foam"):
         assert_bitexact(got[k], want[k], k)
     assert np.array_equal(got["dry"], want["dry"])
-    assert got["dry"].any() and (got["flow_speed"] > 0).any()
+    if W > 1:  # (a 1-wide open grid has drained by now)
+        assert got["dry"].any() and (got["flow_speed"] > 0).any()
 
 
 @pytest.mark.parametrize("W,H,levels", [(64, 48, 3), (100, 37, 2), (256, 256, 8)])

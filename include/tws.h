@@ -112,7 +112,8 @@ typedef struct tws_buffers {
 /* ---- lifecycle -----------------------------------------------------------
  * Replaces Terrain::Terrain + CreateHeightmapFromNoiseAndResetSim's texture
  * allocation (Terrain.cpp:21-132, 200-238).  `stream` is a cudaStream_t
- * (NULL: the library creates one).  State starts as b = d = f = v = 0. */
+ * (NULL: the library creates one).  State starts as b = d = f = v = 0.
+ * 1 <= width <= 2^20, 1 <= height <= 2^19. */
 TWS_API int tws_create(int width, int height, const tws_sim_params* params, int flux_storage,
                        void* stream, tws_grid** out);
 /* Replaces Terrain::~Terrain (Terrain.cpp:134-148). */

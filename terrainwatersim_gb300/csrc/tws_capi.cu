@@ -287,7 +287,9 @@ TWS_API int tws_create(int width, int height, const tws_sim_params* params, int 
                        void* stream, tws_grid** out) {
   if (!out) return TWS_ERR_INVALID;
   *out = nullptr;
-  if (width < 1 || height < 1 || width > (1 << 20) || height > (1 << 20) || !params_ok(params))
+  // (height <= 2^19 keeps the tile rows of a one-CTA-per-tile launch within
+  // the 65535 limit of a grid's y dimension for 16-row tiles)
+  if (width < 1 || height < 1 || width > (1 << 20) || height > (1 << 19) || !params_ok(params))
     return TWS_ERR_INVALID;
   if (flux_storage != TWS_FLUX_F32 && flux_storage != TWS_FLUX_F16) return TWS_ERR_INVALID;
   tws_grid* g = new (std::nothrow) tws_grid();

@@ -180,17 +180,19 @@ __device__ __forceinline__ void process_tile(const StepArgs& a, float* __restric
   const bool closed = a.closed != 0;
 
   // Phase 0: first step's sources, surface height h = d + b (flowUpdate.comp:34).
-  for (int idx = tid; idx < T::NB; idx += kThreads) {
-    float d = sd[idx];
-    if (mask) {
+  if (mask) {
+    for (int idx = tid; idx < T::NB; idx += kThreads) {
+      float d = sd[idx];
       const int i = idx / T::BW, j = idx - (idx / T::BW) * T::BW;
       const int gx = x0 - T::HX + j, gy = y0 - T::HY + i;
       if (INTERIOR || (gx >= 0 && gx < W && gy >= 0 && gy < H)) {
         d = add_sources(d, gx, gy, a, mask);
         sd[idx] = d;
       }
+      sh[idx] = fadd(d, sb[idx]);
     }
-    sh[idx] = fadd(d, sb[idx]);
+  } else {
+    for (int idx = tid; idx < T::NB; idx += kThreads) sh[idx] = fadd(sd[idx], sb[idx]);
   }
   if (F16) {
     const __half2* st = reinterpret_cast<const __half2*>(staging);
@@ -314,8 +316,21 @@ __global__ void __launch_bounds__(kThreads)
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + T::OFF_BAR);
 
   const int tid = threadIdx.x;
-  const int tiles_x = (a.W + TX - 1) / TX;
-  const int num_tiles = tiles_x * ((a.H + TY - 1) / TY);
+  // One CTA per tile (STAGES == 1) takes its tile from a 2-D grid; the
+  // persistent form walks the tiles by a 1-D numbering.
+  const int tiles_x = STAGES == 1 ? 1 : (a.W + TX - 1) / TX;
+  const int num_tiles = STAGES == 1 ? 1 : tiles_x * ((a.H + TY - 1) / TY);
+  const int first = STAGES == 1 ? 0 : (int)blockIdx.x;
+  const int stride = STAGES == 1 ? 1 : (int)gridDim.x;
+  auto tile_origin = [&](int t, int& x0, int& y0) {
+    if (STAGES == 1) {
+      x0 = blockIdx.x * TX;
+      y0 = blockIdx.y * TY;
+    } else {
+      x0 = (t % tiles_x) * TX;
+      y0 = (t / tiles_x) * TY;
+    }
+  };
 
   if (tid == 0) {
 #pragma unroll
@@ -326,15 +341,17 @@ __global__ void __launch_bounds__(kThreads)
   if (tid == 0) {
 #pragma unroll
     for (int s = 0; s < STAGES; ++s) {
-      const int t = blockIdx.x + s * gridDim.x;
-      if (t < num_tiles)
-        issue_tile<T, F16>(smem + s * T::ST_BYTES, &bars[s], &tm_b, &tm_d, &tm_f,
-                           (t % tiles_x) * TX, (t / tiles_x) * TY);
+      const int t = first + s * stride;
+      if (t < num_tiles) {
+        int tx0, ty0;
+        tile_origin(t, tx0, ty0);
+        issue_tile<T, F16>(smem + s * T::ST_BYTES, &bars[s], &tm_b, &tm_d, &tm_f, tx0, ty0);
+      }
     }
   }
 
   int it = 0;
-  for (int t = blockIdx.x; t < num_tiles; t += gridDim.x, ++it) {
+  for (int t = first; t < num_tiles; t += stride, ++it) {
     const int s = STAGES == 1 ? 0 : it % STAGES;
     const uint32_t parity = (uint32_t)((it / STAGES) & 1);
     unsigned char* st = smem + s * T::ST_BYTES;
@@ -343,18 +360,16 @@ __global__ void __launch_bounds__(kThreads)
     float* sh = T::H_ALIAS ? sb : reinterpret_cast<float*>(smem + T::OFF_H);
     float4* sf = F16 ? reinterpret_cast<float4*>(smem + T::OFF_F16)
                      : reinterpret_cast<float4*>(st + T::ST_F);
-    const int x0 = (t % tiles_x) * TX, y0 = (t / tiles_x) * TY;
+    int x0, y0;
+    tile_origin(t, x0, y0);
 
     // Which sources can touch this tile's b/d box.
     uint32_t mask = 0;
-#pragma unroll
-    for (int k = 0; k < TWS_MAX_SOURCES; ++k) {
-      if (k < a.nsrc) {
-        const DevSource& src = a.src[k];
-        if (src.bx1 >= x0 - T::HX && src.bx0 < x0 + TX + T::HX && src.by1 >= y0 - T::HY &&
-            src.by0 < y0 + TY + T::HY)
-          mask |= 1u << k;
-      }
+    for (int k = 0; k < a.nsrc; ++k) {
+      const DevSource& src = a.src[k];
+      if (src.bx1 >= x0 - T::HX && src.bx0 < x0 + TX + T::HX && src.by1 >= y0 - T::HY &&
+          src.by0 < y0 + TY + T::HY)
+        mask |= 1u << k;
     }
 
     const bool ok = wait_bounded(&bars[s], parity, a.err);
@@ -368,12 +383,13 @@ __global__ void __launch_bounds__(kThreads)
                                                   sd, sh, sf, st + T::ST_F);
     __syncthreads();  // stage s, h and the F16 working copy are free again
 
-    if (tid == 0) {
-      const int tn = t + STAGES * gridDim.x;
+    if (STAGES > 1 && tid == 0) {
+      const int tn = t + STAGES * stride;
       if (tn < num_tiles) {
+        int nx0, ny0;
+        tile_origin(tn, nx0, ny0);
         fence_proxy_async_smem();
-        issue_tile<T, F16>(st, &bars[s], &tm_b, &tm_d, &tm_f, (tn % tiles_x) * TX,
-                           (tn / tiles_x) * TY);
+        issue_tile<T, F16>(st, &bars[s], &tm_b, &tm_d, &tm_f, nx0, ny0);
       }
     }
   }
@@ -657,9 +673,9 @@ cudaError_t launch_step(int variant, int flux_storage, const CUtensorMap* tm_b,
     ctas_per_sm = e.ctas_per_sm[fs];
   }
   const StepVariant& v = e.v;
-  const long long tiles = (long long)((a.W + v.tx - 1) / v.tx) * ((a.H + v.ty - 1) / v.ty);
-  long long blocks = tiles;
-  if (v.stages > 1) {
+  const int tiles_x = (a.W + v.tx - 1) / v.tx, tiles_y = (a.H + v.ty - 1) / v.ty;
+  dim3 grid(tiles_x, tiles_y);  // one CTA per tile
+  if (v.stages > 1) {           // persistent: as many CTAs as fit at once
     static int sms = 0;
     if (sms == 0) {
       int dev = 0;
@@ -667,10 +683,12 @@ cudaError_t launch_step(int variant, int flux_storage, const CUtensorMap* tm_b,
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
       if (sms <= 0) sms = 1;
     }
-    blocks = std::min<long long>(tiles, (long long)sms * ctas_per_sm);
+    grid = dim3((unsigned)std::min<long long>((long long)tiles_x * tiles_y,
+                                              (long long)sms * ctas_per_sm));
   }
+  if (grid.y > 65535) return cudaErrorInvalidConfiguration;
   auto kfn = reinterpret_cast<KernelFn>(const_cast<void*>(fn));
-  kfn<<<(unsigned)blocks, kThreads, smem, s>>>(*tm_b, *tm_d, *tm_f, a);
+  kfn<<<grid, kThreads, smem, s>>>(*tm_b, *tm_d, *tm_f, a);
   count_launch();
   return cudaGetLastError();
 }

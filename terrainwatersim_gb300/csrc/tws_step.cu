@@ -395,6 +395,220 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// ---- row tiles: a warp per row band, neighbours by shuffle ---------------------
+// The same K-step tile computation with a mapping chosen for few instructions
+// per cell.  Lane l of every warp owns flux-box column l - 1: the flux box is 30
+// columns wide (output width 32 - 4K plus the 2K-1 halo on each side), so
+// lanes 1..30 compute and lanes 0 and 31 only hold the neighbouring column for
+// the shuffles.  Each warp walks a contiguous band of rows: the surface
+// heights above and below, and the outflow records of the rows above and
+// below, stay in registers, the x neighbours come from the adjacent lanes, and
+// no per-cell index division or bounds arithmetic is left in the loops.
+template <int K, int TY, bool F16>
+struct RowTile {
+  static constexpr int TX = 32 - 4 * K;           // output columns (a multiple of 4)
+  static constexpr int HX = (2 * K + 3) / 4 * 4;  // x halo of b/d, whole 16-byte units
+  static constexpr int HY = 2 * K;
+  static constexpr int BW = TX + 2 * HX, BH = TY + 2 * HY;
+  static constexpr int RF = 2 * K - 1;
+  static constexpr int FW = TX + 2 * RF, FH = TY + 2 * RF;  // FW = 30
+  static constexpr int SW = FW + 2;
+  static constexpr int LC = HX - RF - 1;  // b-box column of lane 0
+  static constexpr int NB = BW * BH, NF = FW * FH;
+  static constexpr bool H_ALIAS = (K == 1);
+  static constexpr size_t ST_B = 0;
+  static constexpr size_t ST_D = align_up((size_t)NB * 4, 128);
+  static constexpr size_t ST_F = align_up(ST_D + (size_t)NB * 4, 128);
+  static constexpr size_t ST_BYTES =
+      align_up(ST_F + (F16 ? (size_t)SW * FH * 8 : (size_t)NF * 16), 128);
+  static constexpr size_t OFF_H = ST_BYTES;
+  static constexpr size_t OFF_F16 = align_up(OFF_H + (H_ALIAS ? 0 : (size_t)NB * 4), 128);
+  static constexpr size_t OFF_BAR = align_up(OFF_F16 + (F16 ? (size_t)NF * 16 : 0), 128);
+  static constexpr size_t SMEM = OFF_BAR + 8 + 128;
+  static constexpr uint32_t TX_BYTES = (uint32_t)(2 * NB * 4 + (F16 ? SW * FH * 8 : NF * 16));
+  static_assert(FW == 30 && LC >= 0 && LC + 31 < BW, "row-tile lane mapping");
+};
+
+template <int K, int TY, bool F16, bool INTERIOR>
+__device__ __forceinline__ void row_process(const StepArgs& a, int x0, int y0, uint32_t mask,
+                                            float* sb, float* sd, float* sh, float4* sf,
+                                            const unsigned char* staging) {
+  using T = RowTile<K, TY, F16>;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int W = a.W, H = a.H;
+  const float kf = a.kf, ka = a.ka, cc = a.c;
+  const float fscale = a.flux_scale, finv = a.flux_inv_scale;
+  const bool closed = a.closed != 0;
+  const int bcol = T::LC + lane;                                   // this lane's b-box column
+  const int fcol = lane == 0 ? 0 : (lane > T::FW ? T::FW - 1 : lane - 1);  // clamped f column
+  const int gxl = x0 - T::RF + lane - 1;                           // this lane's grid column
+
+  // Phase 0: h = d + b over the b-box rows, the 32 columns the lanes read.
+  for (int r = warp; r < T::BH; r += 8) {
+    const int bidx = r * T::BW + bcol;
+    float d = sd[bidx];
+    if (mask) {
+      const int gy = y0 - T::HY + r;
+      if (INTERIOR || (gxl >= 0 && gxl < W && gy >= 0 && gy < H)) {
+        d = add_sources(d, gxl, gy, a, mask);
+        sd[bidx] = d;
+      }
+    }
+    sh[bidx] = fadd(d, sb[bidx]);
+  }
+  if (F16) {
+    const __half2* st = reinterpret_cast<const __half2*>(staging);
+    for (int idx = tid; idx < T::NF; idx += kThreads) {
+      const int i = idx / T::FW, j = idx - (idx / T::FW) * T::FW;
+      const int s = i * T::SW + j + 1;
+      const float2 lo = __half22float2(st[2 * s]), hi = __half22float2(st[2 * s + 1]);
+      sf[idx] = make_float4(fmul(lo.x, finv), fmul(lo.y, finv), fmul(hi.x, finv), fmul(hi.y, finv));
+    }
+  }
+  __syncthreads();
+
+#pragma unroll
+  for (int s = 0; s < K; ++s) {
+    // Phase A: outflow on flux-box rows [2s, FH - 2s), columns [2s, FW - 2s).
+    {
+      const int a0 = 2 * s, a1 = T::FH - 2 * s;
+      const int band = (a1 - a0 + 7) / 8;
+      const int r0 = a0 + warp * band, r1 = min(r0 + band, a1);
+      const bool act = lane >= 2 * s + 1 && lane <= T::FW - 2 * s;
+      if (r0 < r1) {
+        // flux-box row r is b-box row r + 1 (HY = RF + 1)
+        float hm = sh[r0 * T::BW + bcol];
+        float hc = sh[(r0 + 1) * T::BW + bcol];
+        for (int r = r0; r < r1; ++r) {
+          const float hp = sh[(r + 2) * T::BW + bcol];
+          const float hx1 = __shfl_down_sync(0xffffffffu, hc, 1);
+          const float hx0 = __shfl_up_sync(0xffffffffu, hc, 1);
+          const int gy = y0 - T::RF + r;
+          if (act && (INTERIOR || (gxl >= 0 && gxl < W && gy >= 0 && gy < H))) {
+            const float dc = sd[(r + 1) * T::BW + bcol];
+            const int fidx = r * T::FW + fcol;
+            const float4 fo = sf[fidx];
+            float4 nf;
+            nf.x = max0(fadd(fmul(fo.x, kf), fmul(fsub(hc, hx1), ka)));
+            nf.y = max0(fadd(fmul(fo.y, kf), fmul(fsub(hc, hx0), ka)));
+            nf.z = max0(fadd(fmul(fo.z, kf), fmul(fsub(hc, hp), ka)));
+            nf.w = max0(fadd(fmul(fo.w, kf), fmul(fsub(hc, hm), ka)));
+            if (!INTERIOR && closed) {
+              if (gxl + 1 >= W) nf.x = 0.0f;
+              if (gxl == 0) nf.y = 0.0f;
+              if (gy + 1 >= H) nf.z = 0.0f;
+              if (gy == 0) nf.w = 0.0f;
+            }
+            const float total = fmul(fadd(fadd(fadd(nf.x, nf.y), nf.z), nf.w), cc);
+            if (total > dc) {
+              const float sc = fdiv(dc, total);
+              nf.x = fmul(nf.x, sc);
+              nf.y = fmul(nf.y, sc);
+              nf.z = fmul(nf.z, sc);
+              nf.w = fmul(nf.w, sc);
+            }
+            if (F16) {
+              nf.x = quantize_f16(nf.x, fscale, finv);
+              nf.y = quantize_f16(nf.y, fscale, finv);
+              nf.z = quantize_f16(nf.z, fscale, finv);
+              nf.w = quantize_f16(nf.w, fscale, finv);
+            }
+            sf[fidx] = nf;
+          }
+          hm = hc;
+          hc = hp;
+        }
+      }
+    }
+    __syncthreads();
+
+    // Phase B: depth and flow vector on rows [2s + 1, FH - 2s - 1), columns
+    // [2s + 1, FW - 2s - 1).
+    {
+      const int b0 = 2 * s + 1, b1 = T::FH - 2 * s - 1;
+      const int band = (b1 - b0 + 7) / 8;
+      const int r0 = b0 + warp * band, r1 = min(r0 + band, b1);
+      const bool act = lane >= 2 * s + 2 && lane <= T::FW - 2 * s - 1;
+      if (r0 < r1) {
+        float fz_m = sf[(r0 - 1) * T::FW + fcol].z;
+        float4 fc = sf[r0 * T::FW + fcol];
+        for (int r = r0; r < r1; ++r) {
+          const float4 fp = sf[(r + 1) * T::FW + fcol];
+          const float X1 = __shfl_down_sync(0xffffffffu, fc.y, 1);
+          const float X0 = __shfl_up_sync(0xffffffffu, fc.x, 1);
+          const int gy = y0 - T::RF + r;
+          if (act && (INTERIOR || (gxl >= 0 && gxl < W && gy >= 0 && gy < H))) {
+            const float Y1 = fp.w, Y0 = fz_m;
+            const int bidx = (r + 1) * T::BW + bcol;
+            const float in = fadd(fadd(fadd(X1, X0), Y1), Y0);
+            const float out = fadd(fadd(fadd(fc.x, fc.y), fc.z), fc.w);
+            const float dn = max0(fadd(sd[bidx], fmul(fsub(in, out), cc)));
+            if (s == K - 1) {
+              const size_t g = (size_t)gy * a.pitch + gxl;
+              a.d_out[g] = dn;
+              if (F16) {
+                const __half2 lo = __floats2half2_rn(fmul(fc.x, fscale), fmul(fc.y, fscale));
+                const __half2 hi = __floats2half2_rn(fmul(fc.z, fscale), fmul(fc.w, fscale));
+                uint2 packed;
+                packed.x = *reinterpret_cast<const uint32_t*>(&lo);
+                packed.y = *reinterpret_cast<const uint32_t*>(&hi);
+                reinterpret_cast<uint2*>(a.f_out)[g] = packed;
+              } else {
+                reinterpret_cast<float4*>(a.f_out)[g] = fc;
+              }
+              a.v_out[g] = make_float2(fsub(fsub(X1, fc.x), fsub(X0, fc.y)),
+                                       fsub(fsub(Y1, fc.z), fsub(Y0, fc.w)));
+            } else {
+              const float dnext = mask ? add_sources(dn, gxl, gy, a, mask) : dn;
+              sd[bidx] = dnext;
+              sh[bidx] = fadd(dnext, sb[bidx]);
+            }
+          }
+          fz_m = fc.z;
+          fc = fp;
+        }
+      }
+    }
+    if (s < K - 1) __syncthreads();
+  }
+}
+
+template <int K, int TY, bool F16>
+__global__ void __launch_bounds__(kThreads, 4)
+    row_kernel(const __grid_constant__ CUtensorMap tm_b, const __grid_constant__ CUtensorMap tm_d,
+               const __grid_constant__ CUtensorMap tm_f, const __grid_constant__ StepArgs a) {
+  using T = RowTile<K, TY, F16>;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~static_cast<uintptr_t>(127));
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + T::OFF_BAR);
+  float* sb = reinterpret_cast<float*>(smem + T::ST_B);
+  float* sd = reinterpret_cast<float*>(smem + T::ST_D);
+  float* sh = T::H_ALIAS ? sb : reinterpret_cast<float*>(smem + T::OFF_H);
+  float4* sf = F16 ? reinterpret_cast<float4*>(smem + T::OFF_F16)
+                   : reinterpret_cast<float4*>(smem + T::ST_F);
+  const int x0 = blockIdx.x * T::TX, y0 = blockIdx.y * TY;
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) issue_tile<T, F16>(smem, bar, &tm_b, &tm_d, &tm_f, x0, y0);
+  uint32_t mask = 0;
+  for (int k = 0; k < a.nsrc; ++k) {
+    const DevSource& src = a.src[k];
+    if (src.bx1 >= x0 - T::HX && src.bx0 < x0 + T::TX + T::HX && src.by1 >= y0 - T::HY &&
+        src.by0 < y0 + TY + T::HY)
+      mask |= 1u << k;
+  }
+  const bool ok = wait_bounded(bar, 0, a.err);
+  if (__syncthreads_or(!ok)) return;
+  if (x0 - T::HX >= 0 && y0 - T::HY >= 0 && x0 + T::TX + T::HX <= a.W && y0 + TY + T::HY <= a.H)
+    row_process<K, TY, F16, true>(a, x0, y0, mask, sb, sd, sh, sf, smem + T::ST_F);
+  else
+    row_process<K, TY, F16, false>(a, x0, y0, mask, sb, sd, sh, sf, smem + T::ST_F);
+}
+
 // ---- the batched kernel ------------------------------------------------------
 // Makes the tensor-map proxy observe the current contents of a tensor map in
 // global memory (the host rewrites a batch's table between chains).
@@ -539,6 +753,35 @@ struct VariantTable {
     add_stream(64);       // 13 register streaming, 30-column strips x 64 rows
     add_stream(32);       // 14
     add_stream(128);      // 15
+    add_row<1, 32>();     // 16 row tiles: 28 x 32 outputs
+    add_row<2, 32>();     // 17 24 x 32
+    add_row<3, 32>();     // 18 20 x 32
+    add_row<4, 32>();     // 19 16 x 32
+    add_row<2, 64>();     // 20 24 x 64
+    add_row<3, 64>();     // 21 20 x 64
+  }
+  template <int K, int TY>
+  void add_row() {
+    using R32 = RowTile<K, TY, false>;
+    using R16 = RowTile<K, TY, true>;
+    VariantEntry r;
+    r.v.k = K;
+    r.v.tx = R32::TX;
+    r.v.ty = TY;
+    r.v.stages = 1;
+    r.v.kind = kKindTile;
+    r.v.ry = 0;
+    r.v.hx = R32::HX;
+    r.v.bw = R32::BW;
+    r.v.bh = R32::BH;
+    r.v.fw = R32::FW;
+    r.v.fh = R32::FH;
+    r.v.smem = R32::SMEM > R16::SMEM ? R32::SMEM : R16::SMEM;
+    r.fn[TWS_FLUX_F32] = reinterpret_cast<const void*>(&row_kernel<K, TY, false>);
+    r.fn[TWS_FLUX_F16] = reinterpret_cast<const void*>(&row_kernel<K, TY, true>);
+    r.smem[TWS_FLUX_F32] = R32::SMEM;
+    r.smem[TWS_FLUX_F16] = R16::SMEM;
+    e[n++] = r;
   }
   template <int K, int TX, int TY, int STAGES>
   void add() {

@@ -349,7 +349,7 @@ def run_ours(args):
                 "kernel": f"step_kernel<K={best_k},{vinfo[best_v][1]}x{vinfo[best_v][2]}>",
             },
             "variants": {
-                (f"{'plain' if vinfo[i][0] == 1 else 'blocked_k%d' % vinfo[i][0]}"
+                (f"{i}_{'plain' if vinfo[i][0] == 1 else 'blocked_k%d' % vinfo[i][0]}"
                  f"_{vinfo[i][1]}x{vinfo[i][2]}_{'persistent' if vinfo[i][3] > 1 else 'pertile'}"): {
                     "variant": i,
                     "gcell_steps_per_s": round(cells * chain * v["steps"] * ws / v["seconds"] / 1e9,

@@ -173,6 +173,19 @@ TWS_API int tws_variant_info(int variant, int* steps_per_launch, int* tile_x, in
  * grid shape if tws_autotune ran for one, else the steps-per-launch setting). */
 TWS_API int tws_set_variant(tws_grid* grid, int variant);
 
+/* Failure detection (no reference counterpart: the reference's shaders have
+ * no waits that can run out).  A step kernel waits on a barrier for each of
+ * its tile loads; the wait gives up after `sm_cycles` SM clocks (0: the
+ * default, about two seconds), sets the grid's error word and returns
+ * without writing that tile.  The next tws_sync then reports TWS_ERR_TIMEOUT
+ * once and clears the word; the state is undefined after it and must be
+ * uploaded again, and the context stays usable.
+ * tws_test_inject_missing_bytes makes every tile load declare `bytes` more
+ * (a multiple of 16, 0..4096) than it moves, so that each wait runs out:
+ * the test hook for that path.  0 turns it off. */
+TWS_API int tws_set_wait_limit(tws_grid* grid, long long sm_cycles);
+TWS_API int tws_test_inject_missing_bytes(tws_grid* grid, int bytes);
+
 /* Autotuner: times every variant for `trial_steps` steps on this grid's
  * current state (restored afterwards, so the simulation is unchanged), picks
  * the fastest per cell-step, pins it on this grid and records it for every

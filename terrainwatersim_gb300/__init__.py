@@ -106,6 +106,8 @@ def _declare(L):
         "tws_variant_count": ([], i),
         "tws_variant_info": ([i, vp, vp, vp, vp, vp], i),
         "tws_set_variant": ([vp, i], i),
+        "tws_set_wait_limit": ([vp, C.c_longlong], i),
+        "tws_test_inject_missing_bytes": ([vp, i], i),
         "tws_autotune": ([vp, i, vp], i),
         "tws_step": ([vp, i], i),
         "tws_volume": ([vp, vp], i),
@@ -293,6 +295,16 @@ class Grid:
 
     def set_variant(self, variant: int):
         _check(lib().tws_set_variant(self._h, variant), self._h)
+
+    def set_wait_limit(self, sm_cycles: int):
+        """SM clocks a tile-load wait may take before the kernel gives up
+        (0: the default)."""
+        _check(lib().tws_set_wait_limit(self._h, sm_cycles), self._h)
+
+    def test_inject_missing_bytes(self, nbytes: int):
+        """Test hook: every tile load declares `nbytes` more than it moves,
+        so its bounded wait runs out (0 turns it off)."""
+        _check(lib().tws_test_inject_missing_bytes(self._h, nbytes), self._h)
 
     def autotune(self, trial_steps: int = 24) -> int:
         """Time every kernel variant on this grid's state (restored after)

@@ -54,6 +54,8 @@ struct tws_grid {
   double vol_host[1] = {0.0};
   int* err = nullptr;     // device error word
   int err_host[1] = {0};
+  long long wait_cycles = kDefaultWaitCycles;  // SM clocks a tile-load wait may take
+  int missing_tx = 0;     // test hook: bytes each tile load declares but never moves
   tws_batch* batch = nullptr;  // batch this grid belongs to (its stream is the batch's)
   cudaStream_t home_stream = nullptr;
   std::string last_error;
@@ -181,24 +183,13 @@ StepArgs make_step_args(const tws_grid* g) {
   a.flux_scale = g->flux_scale;
   a.flux_inv_scale = 1.0f / g->flux_scale;
   a.err = g->err;
+  a.wait_cycles = g->wait_cycles;
+  a.missing_tx = g->missing_tx;
   return a;
 }
 
 int enqueue_steps(tws_grid* g, int nsteps) {
-  StepArgs a{};
-  a.W = g->W;
-  a.H = g->H;
-  a.pitch = g->pitch;
-  a.kf = g->params.flow_friction_per_step;
-  a.ka = g->params.water_acceleration_per_step;
-  a.c = g->params.cell_area_inv_time_scaled;
-  a.closed = g->params.boundary == TWS_BOUNDARY_CLOSED;
-  a.nsrc = g->nsrc;
-  for (int i = 0; i < g->nsrc; ++i) a.src[i] = make_dev_source(g->src[i]);
-  a.v_out = g->v;
-  a.flux_scale = g->flux_scale;
-  a.flux_inv_scale = 1.0f / g->flux_scale;
-  a.err = g->err;
+  StepArgs a = make_step_args(g);
   const int main_variant = chosen_variant(g);
   const int kmax = step_variant(main_variant).k;
   int left = nsteps;
@@ -497,6 +488,20 @@ TWS_API int tws_set_variant(tws_grid* g, int variant) {
   return TWS_OK;
 }
 
+TWS_API int tws_set_wait_limit(tws_grid* g, long long sm_cycles) {
+  if (!g || sm_cycles < 0) return fail(g, TWS_ERR_INVALID, "wait limit must be >= 0");
+  g->wait_cycles = sm_cycles == 0 ? kDefaultWaitCycles : sm_cycles;
+  return TWS_OK;
+}
+
+TWS_API int tws_test_inject_missing_bytes(tws_grid* g, int bytes) {
+  // a multiple of 16 keeps the declared count a legal transaction size
+  if (!g || bytes < 0 || bytes > 4096 || bytes % 16 != 0)
+    return fail(g, TWS_ERR_INVALID, "missing bytes must be a multiple of 16 in 0..4096");
+  g->missing_tx = bytes;
+  return TWS_OK;
+}
+
 TWS_API int tws_autotune(tws_grid* g, int trial_steps, int* chosen) {
   if (!g || trial_steps < 1) return fail(g, TWS_ERR_INVALID, "trial_steps must be positive");
   const size_t cells = (size_t)g->pitch * g->H;
@@ -660,8 +665,12 @@ TWS_API int tws_sync(tws_grid* g) {
   TWS_CUDA(g, cudaMemcpyAsync(g->err_host, g->err, sizeof(int), cudaMemcpyDeviceToHost, g->stream),
            "error word copy");
   TWS_CUDA(g, cudaStreamSynchronize(g->stream), "sync");
-  if (*g->err_host != kDevErrNone)
+  if (*g->err_host != kDevErrNone) {
+    // report once; the word is cleared so the grid can be reloaded and reused
+    *g->err_host = kDevErrNone;
+    TWS_CUDA(g, cudaMemsetAsync(g->err, 0, sizeof(int), g->stream), "error word reset");
     return fail(g, TWS_ERR_TIMEOUT, "a kernel gave up waiting for its tile loads");
+  }
   return TWS_OK;
 }
 
@@ -1109,8 +1118,12 @@ TWS_API int tws_batch_sync(tws_batch* b) {
           cudaSuccess ||
       cudaStreamSynchronize(b->stream) != cudaSuccess)
     return bfail(b, TWS_ERR_CUDA, "batch sync");
-  if (b->h_err != kDevErrNone)
+  if (b->h_err != kDevErrNone) {
+    b->h_err = kDevErrNone;
+    if (cudaMemsetAsync(b->d_err, 0, sizeof(int), b->stream) != cudaSuccess)
+      return bfail(b, TWS_ERR_CUDA, "error word reset");
     return bfail(b, TWS_ERR_TIMEOUT, "a batched kernel gave up waiting for its tile loads");
+  }
   return TWS_OK;
 }
 

@@ -15,6 +15,41 @@ __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b)
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
 // GLSL max(0, v) = (0 < v) ? v : 0.
 __device__ __forceinline__ float max0(float v) { return (0.0f < v) ? v : 0.0f; }
+// The same max(0, v) in one min/max instruction: max.f32 returns the other
+// operand for a NaN, and fmaxf(-0, +0) is +0 on sm_103a (measured), so the
+// result is the one of max0 for every v.  The GPU tests check it bit for bit
+// against the oracle, signed zeros included.
+__device__ __forceinline__ float max0_fast(float v) { return fmaxf(v, 0.0f); }
+// Divide for the outflow scaling: the dry case (d = +-0, total > 0) is
+// d / total = d exactly, which skips the divide for the common dry cell.
+__device__ __forceinline__ float scale_factor(float d, float total) {
+  return d == 0.0f ? d : fdiv(d, total);
+}
+
+// ---- packed pairs (sm_100 and later: add/sub/mul.rn.f32x2) ---------------------
+// Each lane is the IEEE round-to-nearest result of its own operands, so one
+// pair operation equals two of the scalar helpers above, in half the issue
+// slots.  One rule: never feed an fmul2 result into fadd2 or fsub2.  The
+// assembler contracts that pair into a packed fused multiply-add despite the
+// .rn modifiers and --fmad=false (measured on sm_103a: about half the results
+// then differ in the last bit); add packed products with the scalar fadd.
+#define TWS_F32X2_OP(name, op)                                                         \
+  __device__ __forceinline__ float2 name(float2 a, float2 b) {                        \
+    float2 r;                                                                          \
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\t"                                               \
+        "mov.b64 ra, {%2, %3};\n\t"                                                    \
+        "mov.b64 rb, {%4, %5};\n\t" op                                                 \
+        " rd, ra, rb;\n\t"                                                             \
+        "mov.b64 {%0, %1}, rd;\n\t}"                                                   \
+        : "=f"(r.x), "=f"(r.y)                                                         \
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));                                     \
+    return r;                                                                          \
+  }
+TWS_F32X2_OP(fadd2, "add.rn.f32x2")
+TWS_F32X2_OP(fsub2, "sub.rn.f32x2")
+TWS_F32X2_OP(fmul2, "mul.rn.f32x2")
+#undef TWS_F32X2_OP
+
 // GLSL clamp(v, 0, 1).
 __device__ __forceinline__ float saturate01(float v) {
   const float m = (v < 0.0f) ? 0.0f : v;

@@ -34,6 +34,8 @@ struct StepArgs {
   float flux_scale;      // F16 storage: stored = f * flux_scale
   float flux_inv_scale;  // F16 storage: f = stored * flux_inv_scale
   int* err;              // device error word (bounded-wait time-outs)
+  long long wait_cycles; // bounded waits give up after this many SM clocks
+  int missing_tx;        // test hook: bytes a tile load declares beyond what it moves
 };
 
 // Kernel variants (temporal block depth K x tile).
@@ -46,6 +48,8 @@ struct StepVariant {
   int hx;     // x halo of the b/d boxes (2K rounded up to 4 floats)
   int bw, bh; // b/d box
   int fw, fh; // flux box
+  int sw;     // F16 staging width in cells (whole pairs)
+  int uni;    // unified layout: the flux box is the b/d box
   size_t smem;
 };
 
@@ -80,6 +84,10 @@ cudaError_t launch_batch_step(int variant, int flux_storage, const BatchGrid* gr
 
 // Device error codes written to StepArgs::err.
 enum : int { kDevErrNone = 0, kDevErrWaitTimeout = 1 };
+
+// Default limit of a bounded tile-load wait: about two seconds at 2 GHz, far
+// beyond any real load, short enough that a lost load ends the kernel.
+constexpr long long kDefaultWaitCycles = 4000000000LL;
 
 // Host helpers implemented in tws_step.cu.
 int step_variant_count();

@@ -31,6 +31,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <mutex>
+#include <type_traits>
 
 #include "tws_device.cuh"
 #include "tws_internal.h"
@@ -39,7 +40,6 @@ namespace tws {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr long long kWaitCycles = 4000000000LL;  // bounded-wait limit in SM clocks
 
 // ---- shared memory / TMA / mbarrier primitives -----------------------------
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -90,18 +90,18 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tm, in
       : "memory");
 }
 
-// Bounded wait on phase `parity`: gives up after kWaitCycles SM clocks (about
-// two seconds; a tile load takes microseconds).  On time-out: record the
-// error, wait once more (bounded) so no copy is left writing into shared
+// Bounded wait on phase `parity`: gives up after `limit` SM clocks (by default
+// about two seconds; a tile load takes microseconds).  On time-out: record
+// the error, wait once more (bounded) so no copy is left writing into shared
 // memory, report false.
-__device__ bool wait_bounded(uint64_t* bar, uint32_t parity, int* err) {
+__device__ bool wait_bounded(uint64_t* bar, uint32_t parity, int* err, long long limit) {
   if (mbar_try_wait(bar, parity)) return true;
   const long long t0 = clock64();
   while (!mbar_try_wait(bar, parity)) {
-    if (clock64() - t0 > kWaitCycles) {
+    if (clock64() - t0 > limit) {
       atomicExch(err, kDevErrWaitTimeout);
       const long long t1 = clock64();
-      while (!mbar_try_wait(bar, parity) && clock64() - t1 < kWaitCycles) {
+      while (!mbar_try_wait(bar, parity) && clock64() - t1 < limit) {
       }
       return false;
     }
@@ -112,30 +112,47 @@ __device__ bool wait_bounded(uint64_t* bar, uint32_t parity, int* err) {
 // ---- tile geometry -----------------------------------------------------------
 __host__ __device__ constexpr size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
-template <int K, int TX, int TY, bool F16, int STAGES>
+// UNI = false: the flux box is the (2K-1)-cell halo the K steps need.
+// UNI = true (unified layout): the flux box is the b/d box itself, so b, d,
+// h and f share one row stride and one index per cell; interior tiles then
+// walk their rings as flat runs of that index (process_tile_flat).  It loads
+// a few more flux records per tile (served from L2).
+template <int K, int TX, int TY, bool F16, int STAGES, bool UNI = false>
 struct Tile {
   static constexpr int HX = (2 * K + 3) / 4 * 4;  // x halo of b/d, whole 16-byte units
   static constexpr int HY = 2 * K;                // y halo of b/d
   static constexpr int BW = TX + 2 * HX, BH = TY + 2 * HY;
-  static constexpr int RF = 2 * K - 1;  // flux halo
-  static constexpr int FW = TX + 2 * RF, FH = TY + 2 * RF;
-  static constexpr int SW = FW + 2;  // F16 staging width in cells (starts one cell early)
+  static constexpr int RF = 2 * K - 1;  // flux halo the K steps need
+  // flux box: origin (x0 - FOX, y0 - FOY), FW x FH cells
+  static constexpr int FOX = UNI ? HX : RF, FOY = UNI ? HY : RF;
+  static constexpr int FW = UNI ? BW : TX + 2 * RF, FH = UNI ? BH : TY + 2 * RF;
+  // F16 staging: whole cell pairs from SOFF cells before the flux box (the box
+  // origin must be an even cell; x0 - 2K is, and so is x0 - HX)
+  static constexpr int SOFF = UNI ? 0 : 1;
+  static constexpr int SW = FW + 2 * SOFF;  // staging width in cells
   static constexpr int NB = BW * BH, NF = FW * FH;
+  // flux-box index of the cell at flux-ring coordinates (fi, fj), whose
+  // origin is (x0 - RF, y0 - RF)
+  static constexpr int FOFF = (FOY - RF) * FW + (FOX - RF);
   // One stage = what TMA writes for one tile: b, d and the flux box (float4
-  // records for F32 storage, the raw halves for F16 storage).
+  // records for F32 storage, the raw halves for F16 storage).  In the unified
+  // layout the flux region always has room for NF float records: the F16
+  // halves are widened to floats in place, and interior tiles keep the flux
+  // there as four channel planes of NB floats (process_tile_flat).
   static constexpr size_t ST_B = 0;
   static constexpr size_t ST_D = align_up((size_t)NB * 4, 128);
   static constexpr size_t ST_F = align_up(ST_D + (size_t)NB * 4, 128);
   static constexpr size_t ST_BYTES =
-      align_up(ST_F + (F16 ? (size_t)SW * FH * 8 : (size_t)NF * 16), 128);
-  // Working arrays shared by all stages: surface height h, and for F16 the
-  // float4 copy of the flux.  With one step per launch the terrain is not
-  // needed once h = d + b is formed, so h overwrites b in place (H_ALIAS) and
-  // the tile needs less shared memory (more CTAs per SM).
+      align_up(ST_F + ((F16 && !UNI) ? (size_t)SW * FH * 8 : (size_t)NF * 16), 128);
+  // Working arrays shared by all stages: surface height h, and (F16 storage,
+  // separate layout) the float4 copy of the flux.  With one step per launch
+  // the terrain is not needed once h = d + b is formed, so h overwrites b in
+  // place (H_ALIAS) and the tile needs less shared memory (more CTAs per SM).
   static constexpr bool H_ALIAS = (K == 1);
   static constexpr size_t OFF_H = STAGES * ST_BYTES;
-  static constexpr size_t OFF_F16 = align_up(OFF_H + (H_ALIAS ? 0 : (size_t)NB * 4), 128);
-  static constexpr size_t OFF_BAR = align_up(OFF_F16 + (F16 ? (size_t)NF * 16 : 0), 128);
+  static constexpr size_t OFF_WORK = align_up(OFF_H + (H_ALIAS ? 0 : (size_t)NB * 4), 128);
+  static constexpr size_t OFF_BAR =
+      align_up(OFF_WORK + ((F16 && !UNI) ? (size_t)NF * 16 : 0), 128);
   static constexpr size_t SMEM = OFF_BAR + 8 * STAGES + 128;  // + slack to align the base
   static constexpr uint32_t TX_BYTES = (uint32_t)(2 * NB * 4 + (F16 ? SW * FH * 8 : NF * 16));
 };
@@ -145,32 +162,40 @@ __device__ __forceinline__ float quantize_f16(float v, float scale, float inv_sc
   const float s = fminf(fmul(v, scale), 65504.0f);
   return fmul(__half2float(__float2half_rn(s)), inv_scale);
 }
+__device__ __forceinline__ float2 quantize_f16x2(float2 v, float2 scale, float2 inv_scale) {
+  const float2 s = fmul2(v, scale);
+  const __half2 h = __floats2half2_rn(fminf(s.x, 65504.0f), fminf(s.y, 65504.0f));
+  return fmul2(__half22float2(h), inv_scale);
+}
 
 // The three TMA loads of the tile at (x0, y0) into one stage buffer.
+// `missing` (normally 0) is the test hook of tws_test_inject_missing_bytes:
+// the barrier then expects bytes that never arrive and its wait runs out.
 template <class T, bool F16>
 __device__ __forceinline__ void issue_tile(unsigned char* st, uint64_t* bar,
                                            const CUtensorMap* tm_b, const CUtensorMap* tm_d,
-                                           const CUtensorMap* tm_f, int x0, int y0) {
-  mbar_expect_tx(bar, T::TX_BYTES);
+                                           const CUtensorMap* tm_f, int x0, int y0,
+                                           int missing = 0) {
+  mbar_expect_tx(bar, T::TX_BYTES + (uint32_t)missing);
   tma_load_2d(st + T::ST_B, tm_b, x0 - T::HX, y0 - T::HY, bar);
   tma_load_2d(st + T::ST_D, tm_d, x0 - T::HX, y0 - T::HY, bar);
   if (F16) {
-    // cell pairs; x0 - RF - 1 = x0 - 2K is even
-    tma_load_3d(st + T::ST_F, tm_f, 0, (x0 - T::RF - 1) / 2, y0 - T::RF, bar);
+    // cell pairs; x0 - FOX - SOFF is even
+    tma_load_3d(st + T::ST_F, tm_f, 0, (x0 - T::FOX - T::SOFF) / 2, y0 - T::FOY, bar);
   } else {
-    tma_load_3d(st + T::ST_F, tm_f, 0, x0 - T::RF, y0 - T::RF, bar);
+    tma_load_3d(st + T::ST_F, tm_f, 0, x0 - T::FOX, y0 - T::FOY, bar);
   }
 }
 
 // K steps of one tile whose loads have landed in (sb, sd, sf-or-staging).
 // INTERIOR: the tile's whole b/d box lies inside the grid, so no cell it
 // computes is off the grid or on the border (no bounds or wall checks).
-template <int K, int TX, int TY, bool F16, int STAGES, bool INTERIOR>
+template <int K, int TX, int TY, bool F16, int STAGES, bool UNI, bool INTERIOR>
 __device__ __forceinline__ void process_tile(const StepArgs& a, float* __restrict__ d_out,
                                              void* __restrict__ f_out, float2* __restrict__ v_out,
                                              int x0, int y0, uint32_t mask, float* sb, float* sd,
                                              float* sh, float4* sf, const unsigned char* staging) {
-  using T = Tile<K, TX, TY, F16, STAGES>;
+  using T = Tile<K, TX, TY, F16, STAGES, UNI>;
   const int tid = threadIdx.x;
   // The per-grid scalars, read once (in the batched kernel `a` lives in
   // global memory; in registers the loops below do not reload them).
@@ -194,11 +219,31 @@ __device__ __forceinline__ void process_tile(const StepArgs& a, float* __restric
   } else {
     for (int idx = tid; idx < T::NB; idx += kThreads) sh[idx] = fadd(sd[idx], sb[idx]);
   }
-  if (F16) {
+  if (F16 && UNI) {
+    // The halves of cell p (bytes 8p..8p+7) widen to the float4 at p (bytes
+    // 16p..16p+15) in place.  Going down in rounds of kThreads cells, round c
+    // writes bytes from 16 kThreads c up, which only hold halves of rounds 2c
+    // and up (already read, behind the barrier); round 0 reads all its
+    // halves before any of its writes.
+    constexpr int IT = (T::NF + kThreads - 1) / kThreads;
+    const __half2* st = reinterpret_cast<const __half2*>(staging);
+#pragma unroll
+    for (int it = IT - 1; it >= 0; --it) {
+      const int idx = it * kThreads + tid;
+      float4 w = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      if (idx < T::NF) {
+        const float2 lo = __half22float2(st[2 * idx]), hi = __half22float2(st[2 * idx + 1]);
+        w = make_float4(fmul(lo.x, finv), fmul(lo.y, finv), fmul(hi.x, finv), fmul(hi.y, finv));
+      }
+      if (it == 0) __syncthreads();
+      if (idx < T::NF) sf[idx] = w;
+      __syncthreads();
+    }
+  } else if (F16) {
     const __half2* st = reinterpret_cast<const __half2*>(staging);
     for (int idx = tid; idx < T::NF; idx += kThreads) {
       const int i = idx / T::FW, j = idx - (idx / T::FW) * T::FW;
-      const int s = i * T::SW + j + 1;
+      const int s = i * T::SW + j + T::SOFF;
       const float2 lo = __half22float2(st[2 * s]), hi = __half22float2(st[2 * s + 1]);
       sf[idx] = make_float4(fmul(lo.x, finv), fmul(lo.y, finv), fmul(hi.x, finv),
                             fmul(hi.y, finv));
@@ -226,7 +271,7 @@ __device__ __forceinline__ void process_tile(const StepArgs& a, float* __restric
         const float ey1 = fsub(hc, sh[bidx + T::BW]);
         const float ey0 = fsub(hc, sh[bidx - T::BW]);
         const float dc = sd[bidx];
-        const int fidx = fi * T::FW + fj;
+        const int fidx = fi * T::FW + fj + T::FOFF;
         const float4 fo = sf[fidx];
         float4 nf;
         nf.x = max0(fadd(fmul(fo.x, kf), fmul(ex1, ka)));
@@ -241,7 +286,7 @@ __device__ __forceinline__ void process_tile(const StepArgs& a, float* __restric
         }
         const float total = fmul(fadd(fadd(fadd(nf.x, nf.y), nf.z), nf.w), cc);
         if (total > dc) {
-          const float sc = fdiv(dc, total);
+          const float sc = scale_factor(dc, total);
           nf.x = fmul(nf.x, sc);
           nf.y = fmul(nf.y, sc);
           nf.z = fmul(nf.z, sc);
@@ -266,7 +311,7 @@ __device__ __forceinline__ void process_tile(const StepArgs& a, float* __restric
         const int fi = T::RF - rd + i, fj = T::RF - rd + j;
         const int gx = x0 - T::RF + fj, gy = y0 - T::RF + fi;
         if (!INTERIOR && (gx < 0 || gx >= W || gy < 0 || gy >= H)) continue;
-        const int fidx = fi * T::FW + fj;
+        const int fidx = fi * T::FW + fj + T::FOFF;
         const float4 fc = sf[fidx];
         const float X1 = sf[fidx + 1].y;      // -x outflow of the +x neighbour
         const float X0 = sf[fidx - 1].x;      // +x outflow of the -x neighbour
@@ -304,12 +349,214 @@ __device__ __forceinline__ void process_tile(const StepArgs& a, float* __restric
   }
 }
 
-// ---- the kernel --------------------------------------------------------------
+// Runs body(p) for p = FIRST .. LAST, thread tid taking FIRST + tid,
+// FIRST + tid + kThreads, ...: fully unrolled, so every position's shared
+// memory address is a constant offset from one register.
+template <int FIRST, int LAST, class F>
+__device__ __forceinline__ void ring_for(int tid, F&& body) {
+  constexpr int N = LAST - FIRST + 1;
+  constexpr int FULL = N / kThreads, REM = N % kThreads;
+#pragma unroll
+  for (int it = 0; it < FULL; ++it) body(FIRST + it * kThreads + tid);
+  if (REM > 0 && tid < REM) body(FIRST + FULL * kThreads + tid);
+}
+
+// K steps of an interior tile in the unified layout: b, d, h and f share the
+// box index p = r * BW + c (box row r, column c).  The ring of a phase is
+// the box rows and columns [lo, hi); the phase walks the single run of p from
+// (lo_r, lo_c) to (hi_r - 1, hi_c - 1), which also covers the wrap-around
+// cells between the ring's rows.  Those cells lie outside the ring, so what
+// they compute lands only where no later phase reads (the rings shrink by
+// two cells per step); their neighbour reads stay inside the box.  The runs
+// are compile-time ranges (ring_for), so no 2-D index and no loop counter is
+// computed per cell.
+//
+// The flux is worked on as four channel planes (fx, fy, fz, fw: +x, -x, +y,
+// -y outflow).  The depth update reads one channel of each neighbour; from
+// planes that is one conflict-free shared-memory wavefront per warp, where a
+// float4 record array needs four.  The planes occupy the bytes of the TMA
+// flux box, so the first step's outflow pass reads the box (float4 records,
+// or the F16 halves) into registers, waits for the whole CTA, then writes the
+// planes: no extra shared memory, so as many CTAs fit per SM as before.
+//
+// The cell arithmetic is process_tile's, with channel pairs in packed f32x2
+// operations, so results are identical.
 template <int K, int TX, int TY, bool F16, int STAGES>
+__device__ __forceinline__ void process_tile_flat(const StepArgs& a, float* __restrict__ d_out,
+                                                  void* __restrict__ f_out,
+                                                  float2* __restrict__ v_out, int x0, int y0,
+                                                  uint32_t mask, float* sb, float* sd, float* sh,
+                                                  unsigned char* fbox) {
+  using T = Tile<K, TX, TY, F16, STAGES, true>;
+  constexpr int S = T::BW;
+  static_assert((TX * TY) % kThreads == 0, "the output tile is whole rounds of the CTA");
+  const int tid = threadIdx.x;
+  const float kf = a.kf, ka = a.ka, cc = a.c;
+  const float fscale = a.flux_scale, finv = a.flux_inv_scale;
+  const float2 kf2 = make_float2(kf, kf), ka2 = make_float2(ka, ka);
+  const float2 fscale2 = make_float2(fscale, fscale), finv2 = make_float2(finv, finv);
+  float* const planes = reinterpret_cast<float*>(fbox);
+  float* __restrict__ fx = planes;
+  float* __restrict__ fy = planes + T::NB;
+  float* __restrict__ fz = planes + 2 * T::NB;
+  float* __restrict__ fw = planes + 3 * T::NB;
+  // box index of the first and last cell of ring r (r cells beyond the tile)
+  constexpr auto first = [](int r) { return (T::HY - r) * S + (T::HX - r); };
+  constexpr auto last = [](int r) { return (T::HY + TY + r - 1) * S + (T::HX + TX + r - 1); };
+
+  // Phase 0: first step's sources and h = d + b (flowUpdate.comp:34).
+  if (mask) {
+    ring_for<0, T::NB - 1>(tid, [&](int p) {
+      const int r = p / S;
+      const float d = add_sources(sd[p], x0 - T::HX + (p - r * S), y0 - T::HY + r, a, mask);
+      sd[p] = d;
+      sh[p] = fadd(d, sb[p]);
+    });
+  } else {
+    ring_for<0, T::NB - 1>(tid, [&](int p) { sh[p] = fadd(sd[p], sb[p]); });
+  }
+  __syncthreads();
+
+  // Phase A: outflow flux with non-negativity scaling, flowUpdate.comp:34-62.
+  // Channel pairs (+x, -x) and (+y, -y) go through the packed f32x2 ops.
+  auto outflow = [&](int p, auto s_) -> float4 {
+    constexpr int s = decltype(s_)::value;
+    float4 fo;
+    if constexpr (s > 0) {
+      fo = make_float4(fx[p], fy[p], fz[p], fw[p]);
+    } else if constexpr (F16) {
+      const __half2* st = reinterpret_cast<const __half2*>(fbox);
+      const float2 lo = fmul2(__half22float2(st[2 * p]), finv2);
+      const float2 hi = fmul2(__half22float2(st[2 * p + 1]), finv2);
+      fo = make_float4(lo.x, lo.y, hi.x, hi.y);
+    } else {
+      fo = reinterpret_cast<const float4*>(fbox)[p];
+    }
+    const float hc = sh[p];
+    const float2 hc2 = make_float2(hc, hc);
+    const float2 ex = fsub2(hc2, make_float2(sh[p + 1], sh[p - 1]));  // (+x, -x)
+    const float2 ey = fsub2(hc2, make_float2(sh[p + S], sh[p - S]));  // (+y, -y)
+    const float dc = sd[p];
+    // products in pairs, their sums scalar (a packed add of packed products
+    // would be contracted to a fused multiply-add)
+    const float2 px = fmul2(make_float2(fo.x, fo.y), kf2), qx = fmul2(ex, ka2);
+    const float2 py = fmul2(make_float2(fo.z, fo.w), kf2), qy = fmul2(ey, ka2);
+    float2 nx = make_float2(max0_fast(fadd(px.x, qx.x)), max0_fast(fadd(px.y, qx.y)));
+    float2 ny = make_float2(max0_fast(fadd(py.x, qy.x)), max0_fast(fadd(py.y, qy.y)));
+    const float total = fmul(fadd(fadd(fadd(nx.x, nx.y), ny.x), ny.y), cc);
+    if (total > dc) {
+      const float sc = scale_factor(dc, total);
+      const float2 sc2 = make_float2(sc, sc);
+      nx = fmul2(nx, sc2);
+      ny = fmul2(ny, sc2);
+    }
+    if (F16) {
+      nx = quantize_f16x2(nx, fscale2, finv2);
+      ny = quantize_f16x2(ny, fscale2, finv2);
+    }
+    return make_float4(nx.x, nx.y, ny.x, ny.y);
+  };
+  auto store = [&](int p, float4 f) {
+    fx[p] = f.x;
+    fy[p] = f.y;
+    fz[p] = f.z;
+    fw[p] = f.w;
+  };
+  // (inflow, outflow) of cell p summed side by side, each in the shader's
+  // order: in = ((X1 + X0) + Y1) + Y0 from the neighbours' channels toward p,
+  // out = ((fx + fy) + fz) + fw.
+  auto in_out = [&](int p, float4 fc) {
+    float2 io = fadd2(make_float2(fy[p + 1], fc.x), make_float2(fx[p - 1], fc.y));
+    io = fadd2(io, make_float2(fw[p + S], fc.z));
+    return fadd2(io, make_float2(fz[p - S], fc.w));
+  };
+  // Phase B: depth update, flowApply.comp:32-52, then the next step's sources
+  // and surface height.
+  auto depth = [&](int p) {
+    const float4 fc = make_float4(fx[p], fy[p], fz[p], fw[p]);
+    const float2 io = in_out(p, fc);
+    float dn = max0_fast(fadd(sd[p], fmul(fsub(io.x, io.y), cc)));
+    if (mask) {
+      const int r = p / S;
+      dn = add_sources(dn, x0 - T::HX + (p - r * S), y0 - T::HY + r, a, mask);
+    }
+    sd[p] = dn;
+    sh[p] = fadd(dn, sb[p]);
+  };
+  // The last step's depth ring is the tile itself: depth, flux and flow map
+  // (flowApply.comp:32-52) go out to the grid.
+  auto finish = [&]() {
+    const size_t pitch = (size_t)a.pitch;
+#pragma unroll
+    for (int it = 0; it < TX * TY / kThreads; ++it) {
+      const int idx = it * kThreads + tid;
+      const int i = idx / TX, j = idx % TX;
+      const int p = (T::HY + i) * S + T::HX + j;
+      const float4 fc = make_float4(fx[p], fy[p], fz[p], fw[p]);
+      const float X1 = fy[p + 1];  // -x outflow of the +x neighbour
+      const float X0 = fx[p - 1];  // +x outflow of the -x neighbour
+      const float Y1 = fw[p + S];  // -y outflow of the +y neighbour
+      const float Y0 = fz[p - S];  // +y outflow of the -y neighbour
+      float2 io = fadd2(make_float2(X1, fc.x), make_float2(X0, fc.y));
+      io = fadd2(io, make_float2(Y1, fc.z));
+      io = fadd2(io, make_float2(Y0, fc.w));
+      const float dn = max0_fast(fadd(sd[p], fmul(fsub(io.x, io.y), cc)));
+      const size_t g = (size_t)(y0 + i) * pitch + (size_t)(x0 + j);
+      d_out[g] = dn;
+      if (F16) {
+        const __half2 lo = __float22half2_rn(fmul2(make_float2(fc.x, fc.y), fscale2));
+        const __half2 hi = __float22half2_rn(fmul2(make_float2(fc.z, fc.w), fscale2));
+        uint2 packed;
+        packed.x = *reinterpret_cast<const uint32_t*>(&lo);
+        packed.y = *reinterpret_cast<const uint32_t*>(&hi);
+        reinterpret_cast<uint2*>(f_out)[g] = packed;
+      } else {
+        reinterpret_cast<float4*>(f_out)[g] = fc;
+      }
+      v_out[g] = fsub2(fsub2(make_float2(X1, Y1), make_float2(fc.x, fc.z)),
+                       fsub2(make_float2(X0, Y0), make_float2(fc.y, fc.w)));
+    }
+  };
+  // step s computes the flux on ring RF - 2s and the depth on the ring inside it
+  auto step = [&](auto s_) {
+    constexpr int s = decltype(s_)::value;
+    constexpr int rf = T::RF - 2 * s;
+    if constexpr (s == 0) {
+      // the planes overwrite the box: all reads first, then all writes
+      constexpr int F = first(rf), N = last(rf) - F + 1;
+      constexpr int IT = (N + kThreads - 1) / kThreads;
+      float4 r[IT];
+#pragma unroll
+      for (int it = 0; it < IT; ++it)
+        if (it * kThreads + tid < N) r[it] = outflow(F + it * kThreads + tid, s_);
+      __syncthreads();
+#pragma unroll
+      for (int it = 0; it < IT; ++it)
+        if (it * kThreads + tid < N) store(F + it * kThreads + tid, r[it]);
+    } else {
+      ring_for<first(rf), last(rf)>(tid, [&](int p) { store(p, outflow(p, s_)); });
+    }
+    __syncthreads();
+    if constexpr (s < K - 1) {
+      ring_for<first(rf - 1), last(rf - 1)>(tid, depth);
+      __syncthreads();
+    } else {
+      finish();
+    }
+  };
+  step(std::integral_constant<int, 0>{});
+  if constexpr (K > 1) step(std::integral_constant<int, 1>{});
+  if constexpr (K > 2) step(std::integral_constant<int, 2>{});
+  if constexpr (K > 3) step(std::integral_constant<int, 3>{});
+  static_assert(K <= 4, "steps per launch");
+}
+
+// ---- the kernel --------------------------------------------------------------
+template <int K, int TX, int TY, bool F16, int STAGES, bool UNI>
 __global__ void __launch_bounds__(kThreads)
     step_kernel(const __grid_constant__ CUtensorMap tm_b, const __grid_constant__ CUtensorMap tm_d,
                 const __grid_constant__ CUtensorMap tm_f, const __grid_constant__ StepArgs a) {
-  using T = Tile<K, TX, TY, F16, STAGES>;
+  using T = Tile<K, TX, TY, F16, STAGES, UNI>;
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~static_cast<uintptr_t>(127));
@@ -345,7 +592,8 @@ __global__ void __launch_bounds__(kThreads)
       if (t < num_tiles) {
         int tx0, ty0;
         tile_origin(t, tx0, ty0);
-        issue_tile<T, F16>(smem + s * T::ST_BYTES, &bars[s], &tm_b, &tm_d, &tm_f, tx0, ty0);
+        issue_tile<T, F16>(smem + s * T::ST_BYTES, &bars[s], &tm_b, &tm_d, &tm_f, tx0, ty0,
+                           a.missing_tx);
       }
     }
   }
@@ -358,8 +606,8 @@ __global__ void __launch_bounds__(kThreads)
     float* sb = reinterpret_cast<float*>(st + T::ST_B);
     float* sd = reinterpret_cast<float*>(st + T::ST_D);
     float* sh = T::H_ALIAS ? sb : reinterpret_cast<float*>(smem + T::OFF_H);
-    float4* sf = F16 ? reinterpret_cast<float4*>(smem + T::OFF_F16)
-                     : reinterpret_cast<float4*>(st + T::ST_F);
+    float4* sf = (F16 && !UNI) ? reinterpret_cast<float4*>(smem + T::OFF_WORK)
+                               : reinterpret_cast<float4*>(st + T::ST_F);
     int x0, y0;
     tile_origin(t, x0, y0);
 
@@ -372,15 +620,20 @@ __global__ void __launch_bounds__(kThreads)
         mask |= 1u << k;
     }
 
-    const bool ok = wait_bounded(&bars[s], parity, a.err);
+    const bool ok = wait_bounded(&bars[s], parity, a.err, a.wait_cycles);
     if (__syncthreads_or(!ok)) return;  // every thread leaves together on a time-out
 
-    if (x0 - T::HX >= 0 && y0 - T::HY >= 0 && x0 + TX + T::HX <= a.W && y0 + TY + T::HY <= a.H)
-      process_tile<K, TX, TY, F16, STAGES, true>(a, a.d_out, a.f_out, a.v_out, x0, y0, mask, sb,
-                                                 sd, sh, sf, st + T::ST_F);
-    else
-      process_tile<K, TX, TY, F16, STAGES, false>(a, a.d_out, a.f_out, a.v_out, x0, y0, mask, sb,
-                                                  sd, sh, sf, st + T::ST_F);
+    if (x0 - T::HX >= 0 && y0 - T::HY >= 0 && x0 + TX + T::HX <= a.W && y0 + TY + T::HY <= a.H) {
+      if constexpr (UNI)
+        process_tile_flat<K, TX, TY, F16, STAGES>(a, a.d_out, a.f_out, a.v_out, x0, y0, mask, sb,
+                                                  sd, sh, st + T::ST_F);
+      else
+        process_tile<K, TX, TY, F16, STAGES, UNI, true>(a, a.d_out, a.f_out, a.v_out, x0, y0,
+                                                        mask, sb, sd, sh, sf, st + T::ST_F);
+    } else {
+      process_tile<K, TX, TY, F16, STAGES, UNI, false>(a, a.d_out, a.f_out, a.v_out, x0, y0, mask,
+                                                       sb, sd, sh, sf, st + T::ST_F);
+    }
     __syncthreads();  // stage s, h and the F16 working copy are free again
 
     if (STAGES > 1 && tid == 0) {
@@ -389,224 +642,10 @@ __global__ void __launch_bounds__(kThreads)
         int nx0, ny0;
         tile_origin(tn, nx0, ny0);
         fence_proxy_async_smem();
-        issue_tile<T, F16>(st, &bars[s], &tm_b, &tm_d, &tm_f, nx0, ny0);
+        issue_tile<T, F16>(st, &bars[s], &tm_b, &tm_d, &tm_f, nx0, ny0, a.missing_tx);
       }
     }
   }
-}
-
-// ---- row tiles: a warp per row band, neighbours by shuffle ---------------------
-// The same K-step tile computation with a mapping chosen for few instructions
-// per cell.  Lane l of every warp owns flux-box column l - 1: the flux box is 30
-// columns wide (output width 32 - 4K plus the 2K-1 halo on each side), so
-// lanes 1..30 compute and lanes 0 and 31 only hold the neighbouring column for
-// the shuffles.  Each warp walks a contiguous band of rows: the surface
-// heights above and below, and the outflow records of the rows above and
-// below, stay in registers, the x neighbours come from the adjacent lanes, and
-// no per-cell index division or bounds arithmetic is left in the loops.
-template <int K, int TY, bool F16>
-struct RowTile {
-  static constexpr int TX = 32 - 4 * K;           // output columns (a multiple of 4)
-  static constexpr int HX = (2 * K + 3) / 4 * 4;  // x halo of b/d, whole 16-byte units
-  static constexpr int HY = 2 * K;
-  static constexpr int BW = TX + 2 * HX, BH = TY + 2 * HY;
-  static constexpr int RF = 2 * K - 1;
-  static constexpr int FW = TX + 2 * RF, FH = TY + 2 * RF;  // FW = 30
-  static constexpr int SW = FW + 2;
-  static constexpr int LC = HX - RF - 1;  // b-box column of lane 0
-  static constexpr int NB = BW * BH, NF = FW * FH;
-  static constexpr bool H_ALIAS = (K == 1);
-  static constexpr size_t ST_B = 0;
-  static constexpr size_t ST_D = align_up((size_t)NB * 4, 128);
-  static constexpr size_t ST_F = align_up(ST_D + (size_t)NB * 4, 128);
-  static constexpr size_t ST_BYTES =
-      align_up(ST_F + (F16 ? (size_t)SW * FH * 8 : (size_t)NF * 16), 128);
-  static constexpr size_t OFF_H = ST_BYTES;
-  static constexpr size_t OFF_F16 = align_up(OFF_H + (H_ALIAS ? 0 : (size_t)NB * 4), 128);
-  static constexpr size_t OFF_BAR = align_up(OFF_F16 + (F16 ? (size_t)NF * 16 : 0), 128);
-  static constexpr size_t SMEM = OFF_BAR + 8 + 128;
-  static constexpr uint32_t TX_BYTES = (uint32_t)(2 * NB * 4 + (F16 ? SW * FH * 8 : NF * 16));
-  static_assert(FW == 30 && LC >= 0 && LC + 31 < BW, "row-tile lane mapping");
-};
-
-template <int K, int TY, bool F16, bool INTERIOR>
-__device__ __forceinline__ void row_process(const StepArgs& a, int x0, int y0, uint32_t mask,
-                                            float* sb, float* sd, float* sh, float4* sf,
-                                            const unsigned char* staging) {
-  using T = RowTile<K, TY, F16>;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int W = a.W, H = a.H;
-  const float kf = a.kf, ka = a.ka, cc = a.c;
-  const float fscale = a.flux_scale, finv = a.flux_inv_scale;
-  const bool closed = a.closed != 0;
-  const int bcol = T::LC + lane;                                   // this lane's b-box column
-  const int fcol = lane == 0 ? 0 : (lane > T::FW ? T::FW - 1 : lane - 1);  // clamped f column
-  const int gxl = x0 - T::RF + lane - 1;                           // this lane's grid column
-
-  // Phase 0: h = d + b over the b-box rows, the 32 columns the lanes read.
-  for (int r = warp; r < T::BH; r += 8) {
-    const int bidx = r * T::BW + bcol;
-    float d = sd[bidx];
-    if (mask) {
-      const int gy = y0 - T::HY + r;
-      if (INTERIOR || (gxl >= 0 && gxl < W && gy >= 0 && gy < H)) {
-        d = add_sources(d, gxl, gy, a, mask);
-        sd[bidx] = d;
-      }
-    }
-    sh[bidx] = fadd(d, sb[bidx]);
-  }
-  if (F16) {
-    const __half2* st = reinterpret_cast<const __half2*>(staging);
-    for (int idx = tid; idx < T::NF; idx += kThreads) {
-      const int i = idx / T::FW, j = idx - (idx / T::FW) * T::FW;
-      const int s = i * T::SW + j + 1;
-      const float2 lo = __half22float2(st[2 * s]), hi = __half22float2(st[2 * s + 1]);
-      sf[idx] = make_float4(fmul(lo.x, finv), fmul(lo.y, finv), fmul(hi.x, finv), fmul(hi.y, finv));
-    }
-  }
-  __syncthreads();
-
-#pragma unroll
-  for (int s = 0; s < K; ++s) {
-    // Phase A: outflow on flux-box rows [2s, FH - 2s), columns [2s, FW - 2s).
-    {
-      const int a0 = 2 * s, a1 = T::FH - 2 * s;
-      const int band = (a1 - a0 + 7) / 8;
-      const int r0 = a0 + warp * band, r1 = min(r0 + band, a1);
-      const bool act = lane >= 2 * s + 1 && lane <= T::FW - 2 * s;
-      if (r0 < r1) {
-        // flux-box row r is b-box row r + 1 (HY = RF + 1)
-        float hm = sh[r0 * T::BW + bcol];
-        float hc = sh[(r0 + 1) * T::BW + bcol];
-        for (int r = r0; r < r1; ++r) {
-          const float hp = sh[(r + 2) * T::BW + bcol];
-          const float hx1 = __shfl_down_sync(0xffffffffu, hc, 1);
-          const float hx0 = __shfl_up_sync(0xffffffffu, hc, 1);
-          const int gy = y0 - T::RF + r;
-          if (act && (INTERIOR || (gxl >= 0 && gxl < W && gy >= 0 && gy < H))) {
-            const float dc = sd[(r + 1) * T::BW + bcol];
-            const int fidx = r * T::FW + fcol;
-            const float4 fo = sf[fidx];
-            float4 nf;
-            nf.x = max0(fadd(fmul(fo.x, kf), fmul(fsub(hc, hx1), ka)));
-            nf.y = max0(fadd(fmul(fo.y, kf), fmul(fsub(hc, hx0), ka)));
-            nf.z = max0(fadd(fmul(fo.z, kf), fmul(fsub(hc, hp), ka)));
-            nf.w = max0(fadd(fmul(fo.w, kf), fmul(fsub(hc, hm), ka)));
-            if (!INTERIOR && closed) {
-              if (gxl + 1 >= W) nf.x = 0.0f;
-              if (gxl == 0) nf.y = 0.0f;
-              if (gy + 1 >= H) nf.z = 0.0f;
-              if (gy == 0) nf.w = 0.0f;
-            }
-            const float total = fmul(fadd(fadd(fadd(nf.x, nf.y), nf.z), nf.w), cc);
-            if (total > dc) {
-              const float sc = fdiv(dc, total);
-              nf.x = fmul(nf.x, sc);
-              nf.y = fmul(nf.y, sc);
-              nf.z = fmul(nf.z, sc);
-              nf.w = fmul(nf.w, sc);
-            }
-            if (F16) {
-              nf.x = quantize_f16(nf.x, fscale, finv);
-              nf.y = quantize_f16(nf.y, fscale, finv);
-              nf.z = quantize_f16(nf.z, fscale, finv);
-              nf.w = quantize_f16(nf.w, fscale, finv);
-            }
-            sf[fidx] = nf;
-          }
-          hm = hc;
-          hc = hp;
-        }
-      }
-    }
-    __syncthreads();
-
-    // Phase B: depth and flow vector on rows [2s + 1, FH - 2s - 1), columns
-    // [2s + 1, FW - 2s - 1).
-    {
-      const int b0 = 2 * s + 1, b1 = T::FH - 2 * s - 1;
-      const int band = (b1 - b0 + 7) / 8;
-      const int r0 = b0 + warp * band, r1 = min(r0 + band, b1);
-      const bool act = lane >= 2 * s + 2 && lane <= T::FW - 2 * s - 1;
-      if (r0 < r1) {
-        float fz_m = sf[(r0 - 1) * T::FW + fcol].z;
-        float4 fc = sf[r0 * T::FW + fcol];
-        for (int r = r0; r < r1; ++r) {
-          const float4 fp = sf[(r + 1) * T::FW + fcol];
-          const float X1 = __shfl_down_sync(0xffffffffu, fc.y, 1);
-          const float X0 = __shfl_up_sync(0xffffffffu, fc.x, 1);
-          const int gy = y0 - T::RF + r;
-          if (act && (INTERIOR || (gxl >= 0 && gxl < W && gy >= 0 && gy < H))) {
-            const float Y1 = fp.w, Y0 = fz_m;
-            const int bidx = (r + 1) * T::BW + bcol;
-            const float in = fadd(fadd(fadd(X1, X0), Y1), Y0);
-            const float out = fadd(fadd(fadd(fc.x, fc.y), fc.z), fc.w);
-            const float dn = max0(fadd(sd[bidx], fmul(fsub(in, out), cc)));
-            if (s == K - 1) {
-              const size_t g = (size_t)gy * a.pitch + gxl;
-              a.d_out[g] = dn;
-              if (F16) {
-                const __half2 lo = __floats2half2_rn(fmul(fc.x, fscale), fmul(fc.y, fscale));
-                const __half2 hi = __floats2half2_rn(fmul(fc.z, fscale), fmul(fc.w, fscale));
-                uint2 packed;
-                packed.x = *reinterpret_cast<const uint32_t*>(&lo);
-                packed.y = *reinterpret_cast<const uint32_t*>(&hi);
-                reinterpret_cast<uint2*>(a.f_out)[g] = packed;
-              } else {
-                reinterpret_cast<float4*>(a.f_out)[g] = fc;
-              }
-              a.v_out[g] = make_float2(fsub(fsub(X1, fc.x), fsub(X0, fc.y)),
-                                       fsub(fsub(Y1, fc.z), fsub(Y0, fc.w)));
-            } else {
-              const float dnext = mask ? add_sources(dn, gxl, gy, a, mask) : dn;
-              sd[bidx] = dnext;
-              sh[bidx] = fadd(dnext, sb[bidx]);
-            }
-          }
-          fz_m = fc.z;
-          fc = fp;
-        }
-      }
-    }
-    if (s < K - 1) __syncthreads();
-  }
-}
-
-template <int K, int TY, bool F16>
-__global__ void __launch_bounds__(kThreads, 4)
-    row_kernel(const __grid_constant__ CUtensorMap tm_b, const __grid_constant__ CUtensorMap tm_d,
-               const __grid_constant__ CUtensorMap tm_f, const __grid_constant__ StepArgs a) {
-  using T = RowTile<K, TY, F16>;
-  extern __shared__ unsigned char smem_raw[];
-  unsigned char* smem = reinterpret_cast<unsigned char*>(
-      (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~static_cast<uintptr_t>(127));
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + T::OFF_BAR);
-  float* sb = reinterpret_cast<float*>(smem + T::ST_B);
-  float* sd = reinterpret_cast<float*>(smem + T::ST_D);
-  float* sh = T::H_ALIAS ? sb : reinterpret_cast<float*>(smem + T::OFF_H);
-  float4* sf = F16 ? reinterpret_cast<float4*>(smem + T::OFF_F16)
-                   : reinterpret_cast<float4*>(smem + T::ST_F);
-  const int x0 = blockIdx.x * T::TX, y0 = blockIdx.y * TY;
-  if (threadIdx.x == 0) {
-    mbar_init(bar, 1);
-    fence_mbar_init();
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) issue_tile<T, F16>(smem, bar, &tm_b, &tm_d, &tm_f, x0, y0);
-  uint32_t mask = 0;
-  for (int k = 0; k < a.nsrc; ++k) {
-    const DevSource& src = a.src[k];
-    if (src.bx1 >= x0 - T::HX && src.bx0 < x0 + T::TX + T::HX && src.by1 >= y0 - T::HY &&
-        src.by0 < y0 + TY + T::HY)
-      mask |= 1u << k;
-  }
-  const bool ok = wait_bounded(bar, 0, a.err);
-  if (__syncthreads_or(!ok)) return;
-  if (x0 - T::HX >= 0 && y0 - T::HY >= 0 && x0 + T::TX + T::HX <= a.W && y0 + TY + T::HY <= a.H)
-    row_process<K, TY, F16, true>(a, x0, y0, mask, sb, sd, sh, sf, smem + T::ST_F);
-  else
-    row_process<K, TY, F16, false>(a, x0, y0, mask, sb, sd, sh, sf, smem + T::ST_F);
 }
 
 // ---- the batched kernel ------------------------------------------------------
@@ -624,11 +663,11 @@ __device__ __forceinline__ void tensormap_acquire(const void* tm) {
 // through that grid's tensor maps and run the same per-tile steps as
 // step_kernel.  Launch `launch_idx` of a chain skips grids that have taken
 // all their launches, so grids with different step counts share a chain.
-template <int K, int TX, int TY, bool F16>
-__global__ void __launch_bounds__(kThreads, 5)
+template <int K, int TX, int TY, bool F16, bool UNI>
+__global__ void __launch_bounds__(kThreads, K >= 3 ? 3 : (UNI ? 4 : 5))
     batch_kernel(const BatchGrid* __restrict__ grids, const int* __restrict__ unit_base,
                  const int* __restrict__ hdr, int launch_idx) {
-  using T = Tile<K, TX, TY, F16, 1>;
+  using T = Tile<K, TX, TY, F16, 1, UNI>;
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~static_cast<uintptr_t>(127));
@@ -636,8 +675,8 @@ __global__ void __launch_bounds__(kThreads, 5)
   float* sb = reinterpret_cast<float*>(smem + T::ST_B);
   float* sd = reinterpret_cast<float*>(smem + T::ST_D);
   float* sh = T::H_ALIAS ? sb : reinterpret_cast<float*>(smem + T::OFF_H);
-  float4* sf = F16 ? reinterpret_cast<float4*>(smem + T::OFF_F16)
-                   : reinterpret_cast<float4*>(smem + T::ST_F);
+  float4* sf = (F16 && !UNI) ? reinterpret_cast<float4*>(smem + T::OFF_WORK)
+                             : reinterpret_cast<float4*>(smem + T::ST_F);
   const int tid = threadIdx.x;
   const int ngrids = hdr[0];
   const int total = unit_base[ngrids];
@@ -667,7 +706,7 @@ __global__ void __launch_bounds__(kThreads, 5)
       tensormap_acquire(&G.tm_b);
       tensormap_acquire(&G.tm_d[p]);
       tensormap_acquire(&G.tm_f[p]);
-      issue_tile<T, F16>(smem, bar, &G.tm_b, &G.tm_d[p], &G.tm_f[p], x0, y0);
+      issue_tile<T, F16>(smem, bar, &G.tm_b, &G.tm_d[p], &G.tm_f[p], x0, y0, a.missing_tx);
     }
     uint32_t mask = 0;
 #pragma unroll
@@ -679,16 +718,21 @@ __global__ void __launch_bounds__(kThreads, 5)
           mask |= 1u << k;
       }
     }
-    const bool ok = wait_bounded(bar, it & 1u, a.err);
+    const bool ok = wait_bounded(bar, it & 1u, a.err, a.wait_cycles);
     ++it;
     if (__syncthreads_or(!ok)) return;
     const int gw = a.W, gh = a.H;
-    if (x0 - T::HX >= 0 && y0 - T::HY >= 0 && x0 + TX + T::HX <= gw && y0 + TY + T::HY <= gh)
-      process_tile<K, TX, TY, F16, 1, true>(a, G.d[p ^ 1], G.f[p ^ 1], G.v, x0, y0, mask, sb, sd,
-                                            sh, sf, smem + T::ST_F);
-    else
-      process_tile<K, TX, TY, F16, 1, false>(a, G.d[p ^ 1], G.f[p ^ 1], G.v, x0, y0, mask, sb, sd,
-                                             sh, sf, smem + T::ST_F);
+    if (x0 - T::HX >= 0 && y0 - T::HY >= 0 && x0 + TX + T::HX <= gw && y0 + TY + T::HY <= gh) {
+      if constexpr (UNI)
+        process_tile_flat<K, TX, TY, F16, 1>(a, G.d[p ^ 1], G.f[p ^ 1], G.v, x0, y0, mask, sb, sd,
+                                             sh, smem + T::ST_F);
+      else
+        process_tile<K, TX, TY, F16, 1, UNI, true>(a, G.d[p ^ 1], G.f[p ^ 1], G.v, x0, y0, mask,
+                                                   sb, sd, sh, sf, smem + T::ST_F);
+    } else {
+      process_tile<K, TX, TY, F16, 1, UNI, false>(a, G.d[p ^ 1], G.f[p ^ 1], G.v, x0, y0, mask, sb,
+                                                  sd, sh, sf, smem + T::ST_F);
+    }
     __syncthreads();  // the tile buffers are free again
   }
 }
@@ -704,10 +748,10 @@ struct VariantEntry {
   bool attr_set[2] = {false, false};
 };
 
-template <int K, int TX, int TY, int STAGES>
+template <int K, int TX, int TY, int STAGES, bool UNI>
 VariantEntry make_entry() {
-  using T32 = Tile<K, TX, TY, false, STAGES>;
-  using T16 = Tile<K, TX, TY, true, STAGES>;
+  using T32 = Tile<K, TX, TY, false, STAGES, UNI>;
+  using T16 = Tile<K, TX, TY, true, STAGES, UNI>;
   VariantEntry e;
   e.v.k = K;
   e.v.tx = TX;
@@ -720,9 +764,11 @@ VariantEntry make_entry() {
   e.v.bh = T32::BH;
   e.v.fw = T32::FW;
   e.v.fh = T32::FH;
+  e.v.sw = T32::SW;
+  e.v.uni = UNI;
   e.v.smem = T32::SMEM > T16::SMEM ? T32::SMEM : T16::SMEM;
-  e.fn[TWS_FLUX_F32] = reinterpret_cast<const void*>(&step_kernel<K, TX, TY, false, STAGES>);
-  e.fn[TWS_FLUX_F16] = reinterpret_cast<const void*>(&step_kernel<K, TX, TY, true, STAGES>);
+  e.fn[TWS_FLUX_F32] = reinterpret_cast<const void*>(&step_kernel<K, TX, TY, false, STAGES, UNI>);
+  e.fn[TWS_FLUX_F16] = reinterpret_cast<const void*>(&step_kernel<K, TX, TY, true, STAGES, UNI>);
   e.smem[TWS_FLUX_F32] = T32::SMEM;
   e.smem[TWS_FLUX_F16] = T16::SMEM;
   return e;
@@ -753,39 +799,18 @@ struct VariantTable {
     add_stream(64);       // 13 register streaming, 30-column strips x 64 rows
     add_stream(32);       // 14
     add_stream(128);      // 15
-    add_row<1, 32>();     // 16 row tiles: 28 x 32 outputs
-    add_row<2, 32>();     // 17 24 x 32
-    add_row<3, 32>();     // 18 20 x 32
-    add_row<4, 32>();     // 19 16 x 32
-    add_row<2, 64>();     // 20 24 x 64
-    add_row<3, 64>();     // 21 20 x 64
+    // unified layout: flux box = b/d box, interior tiles walk flat runs
+    add<2, 32, 32, 1, true>();  // 16
+    add<2, 64, 16, 1, true>();  // 17
+    add<3, 32, 32, 1, true>();  // 18
+    add<3, 64, 16, 1, true>();  // 19
+    add<4, 32, 32, 1, true>();  // 20
+    add<4, 64, 16, 1, true>();  // 21
+    add<3, 64, 32, 1, true>();  // 22
   }
-  template <int K, int TY>
-  void add_row() {
-    using R32 = RowTile<K, TY, false>;
-    using R16 = RowTile<K, TY, true>;
-    VariantEntry r;
-    r.v.k = K;
-    r.v.tx = R32::TX;
-    r.v.ty = TY;
-    r.v.stages = 1;
-    r.v.kind = kKindTile;
-    r.v.ry = 0;
-    r.v.hx = R32::HX;
-    r.v.bw = R32::BW;
-    r.v.bh = R32::BH;
-    r.v.fw = R32::FW;
-    r.v.fh = R32::FH;
-    r.v.smem = R32::SMEM > R16::SMEM ? R32::SMEM : R16::SMEM;
-    r.fn[TWS_FLUX_F32] = reinterpret_cast<const void*>(&row_kernel<K, TY, false>);
-    r.fn[TWS_FLUX_F16] = reinterpret_cast<const void*>(&row_kernel<K, TY, true>);
-    r.smem[TWS_FLUX_F32] = R32::SMEM;
-    r.smem[TWS_FLUX_F16] = R16::SMEM;
-    e[n++] = r;
-  }
-  template <int K, int TX, int TY, int STAGES>
+  template <int K, int TX, int TY, int STAGES, bool UNI = false>
   void add() {
-    e[n++] = make_entry<K, TX, TY, STAGES>();
+    e[n++] = make_entry<K, TX, TY, STAGES, UNI>();
   }
   void add_stream(int ry) {
     VariantEntry s{};
@@ -873,11 +898,11 @@ cudaError_t encode_step_maps(int variant, int flux_storage, int W, int H, int pi
               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     } else {
       // 3-D half {8 = two cells x 4 channels, ceil(W/2) cell pairs, H}.  The
-      // box starts one cell before the flux halo so its x coordinate is whole
-      // pairs; the padding cell of an odd-width row is kept at zero.
+      // box (the staging width, whole pairs) starts on an even cell; the
+      // padding cell of an odd-width row is kept at zero.
       const cuuint64_t gdim[3] = {8, (cuuint64_t)((W + 1) / 2), (cuuint64_t)H};
       const cuuint64_t gstr[2] = {16, (cuuint64_t)pitch * 8};
-      const cuuint32_t box[3] = {8, (cuuint32_t)((v.fw + 2) / 2), (cuuint32_t)v.fh};
+      const cuuint32_t box[3] = {8, (cuuint32_t)(v.sw / 2), (cuuint32_t)v.fh};
       r = enc(tm_f, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, const_cast<void*>(f), gdim, gstr, box,
               estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -942,24 +967,26 @@ namespace {
 using BatchFn = void (*)(const BatchGrid*, const int*, const int*, int);
 
 struct BatchEntry {
-  int k, tx, ty, step_variant;  // step_variant: the single-grid variant with the same boxes
+  int k, tx, ty, uni;
+  int step_variant;  // the single-grid variant with the same boxes (its tensor maps fit)
   const void* fn[2];
   size_t smem[2];
   int ctas_per_sm[2] = {0, 0};
   bool set[2] = {false, false};
 };
 
-template <int K, int TX, int TY>
+template <int K, int TX, int TY, bool UNI>
 BatchEntry make_batch_entry(int step_variant) {
   BatchEntry e;
   e.k = K;
   e.tx = TX;
   e.ty = TY;
+  e.uni = UNI;
   e.step_variant = step_variant;
-  e.fn[TWS_FLUX_F32] = reinterpret_cast<const void*>(&batch_kernel<K, TX, TY, false>);
-  e.fn[TWS_FLUX_F16] = reinterpret_cast<const void*>(&batch_kernel<K, TX, TY, true>);
-  e.smem[TWS_FLUX_F32] = Tile<K, TX, TY, false, 1>::SMEM;
-  e.smem[TWS_FLUX_F16] = Tile<K, TX, TY, true, 1>::SMEM;
+  e.fn[TWS_FLUX_F32] = reinterpret_cast<const void*>(&batch_kernel<K, TX, TY, false, UNI>);
+  e.fn[TWS_FLUX_F16] = reinterpret_cast<const void*>(&batch_kernel<K, TX, TY, true, UNI>);
+  e.smem[TWS_FLUX_F32] = Tile<K, TX, TY, false, 1, UNI>::SMEM;
+  e.smem[TWS_FLUX_F16] = Tile<K, TX, TY, true, 1, UNI>::SMEM;
   return e;
 }
 
@@ -968,10 +995,13 @@ struct BatchTable {
   int n = 0;
   std::mutex mu;
   BatchTable() {
-    e[n++] = make_batch_entry<1, 32, 32>(0);
-    e[n++] = make_batch_entry<2, 32, 32>(10);
-    e[n++] = make_batch_entry<1, 64, 16>(4);
-    e[n++] = make_batch_entry<2, 64, 16>(1);
+    e[n++] = make_batch_entry<1, 32, 32, false>(0);
+    e[n++] = make_batch_entry<2, 32, 32, false>(10);
+    e[n++] = make_batch_entry<1, 64, 16, false>(4);
+    e[n++] = make_batch_entry<2, 64, 16, false>(1);
+    e[n++] = make_batch_entry<2, 32, 32, true>(16);
+    e[n++] = make_batch_entry<2, 64, 16, true>(17);
+    e[n++] = make_batch_entry<3, 32, 32, true>(18);
   }
 };
 
@@ -997,6 +1027,9 @@ cudaError_t prepare_batch_variant(int variant, int flux_storage) {
   if (variant < 0 || variant >= t.n) return cudaErrorInvalidValue;
   const int fs = flux_storage == TWS_FLUX_F16 ? TWS_FLUX_F16 : TWS_FLUX_F32;
   BatchEntry& e = t.e[variant];
+  const StepVariant& sv = step_variant(e.step_variant);
+  if (sv.k != e.k || sv.tx != e.tx || sv.ty != e.ty || sv.uni != e.uni || sv.stages != 1)
+    return cudaErrorInvalidValue;  // the tables disagree: the maps would not fit
   std::lock_guard<std::mutex> lk(t.mu);
   if (!e.set[fs]) {
     cudaError_t err =

@@ -268,10 +268,11 @@ def test_error_paths(tws):
 
 # ------------------------------------------------------------ variants and autotuner
 
-@pytest.mark.parametrize("W,H", [(97, 130), (300, 41), (1, 70)])
+@pytest.mark.parametrize("W,H", [(97, 130), (300, 41), (1, 70), (260, 200)])
 def test_every_kernel_variant_bitexact(tws, oracle, W, H):
     """Every (temporal depth, tile) variant, with a step count that leaves a
-    remainder for the shallower kernels, matches the oracle bit for bit."""
+    remainder for the shallower kernels, matches the oracle bit for bit.
+    260 x 200 gives every tile shape interior tiles, some under the source."""
     rng = np.random.default_rng(W + 7 * H)
     b = rng.uniform(0, 6, (H, W)).astype(np.float32)
     d = np.maximum(0, rng.uniform(-2, 5, (H, W))).astype(np.float32)
@@ -289,6 +290,42 @@ def test_every_kernel_variant_bitexact(tws, oracle, W, H):
         assert_bitexact(gd, od, f"depth variant {vi}")
         assert_bitexact(gf, of, f"flux variant {vi}")
         assert_bitexact(gv, ov, f"velocity variant {vi}")
+
+
+def test_signed_zeros_bitexact_every_variant(tws, oracle):
+    """A patch where terrain, depth and flux are zeros of random sign, in
+    a grid with interior tiles: surface differences of -0, flux terms of -0
+    and dry cells that must scale to zero.  Every variant keeps the signs the
+    shaders give (max(0, v) of -0 is +0; a dry cell's scale is its depth)."""
+    W, H = 200, 160
+    rng = np.random.default_rng(17)
+    b = rng.uniform(0, 3, (H, W)).astype(np.float32)
+    d = rng.uniform(0, 2, (H, W)).astype(np.float32)
+    f = rng.uniform(0, 0.2, (H, W, 4)).astype(np.float32)
+
+    def signed_zeros(shape):
+        return np.where(rng.random(shape) < 0.5, np.float32(-0.0), np.float32(0.0))
+
+    ys, xs = slice(40, 120), slice(50, 150)
+    b[ys, xs] = signed_zeros(b[ys, xs].shape)
+    d[ys, xs] = signed_zeros(d[ys, xs].shape)
+    f[ys, xs] = signed_zeros(f[ys, xs].shape)
+    # scattered dry cells with signed-zero depth elsewhere
+    dry = rng.random((H, W)) < 0.2
+    d[dry] = signed_zeros(int(dry.sum()))
+    assert np.signbit(d).any() and np.signbit(f).any()
+    p = tws.params_physical(boundary=tws.BOUNDARY_CLOSED)
+    for steps in (1, 4):
+        od, of, ov = oracle_run(oracle, b, d, f, p.as_tuple(), [], steps, oracle.BOUNDARY_CLOSED)
+        for vi in range(len(tws.variants())):
+            with tws.Grid(W, H, p) as g:
+                g.upload(b, d, f)
+                g.set_variant(vi)
+                g.step(steps)
+                gd, gf, gv = g.download()
+            assert_bitexact(gd, od, f"depth variant {vi}, {steps} steps")
+            assert_bitexact(gf, of, f"flux variant {vi}, {steps} steps")
+            assert_bitexact(gv, ov, f"velocity variant {vi}, {steps} steps")
 
 
 def test_autotune_preserves_state_and_pins_a_variant(tws, oracle):

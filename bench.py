@@ -654,7 +654,7 @@ def run_c3(args):
             round(cells * steps / plain_streams_s / 1e9, 3),
         "speedup_vs_one_grid_at_a_time": round(plain_s / batch_s, 3),
         "speedup_vs_concurrent_streams": round(plain_streams_s / batch_s, 3),
-        "batched_variant": tws.batch_variants()[tuned],
+        "batched_variant": {"index": tuned, "k_tile": tws.batch_variants()[tuned]},
         "chains": chains, "graph_replays": replayed,
         "fp64_checks": checks,
     }

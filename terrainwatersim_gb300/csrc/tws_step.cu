@@ -90,6 +90,13 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tm, in
       : "memory");
 }
 
+// The dynamic shared memory base rounded up to 128 bytes (TMA destinations),
+// by pointer arithmetic on the shared array so the compiler keeps every access
+// derived from it in the shared window (LDS/STS, not generic loads).
+__device__ __forceinline__ unsigned char* align_smem(unsigned char* raw) {
+  return raw + ((128u - (smem_u32(raw) & 127u)) & 127u);
+}
+
 // Bounded wait on phase `parity`: gives up after `limit` SM clocks (by default
 // about two seconds; a tile load takes microseconds).  On time-out: record
 // the error, wait once more (bounded) so no copy is left writing into shared
@@ -557,9 +564,8 @@ __global__ void __launch_bounds__(kThreads)
     step_kernel(const __grid_constant__ CUtensorMap tm_b, const __grid_constant__ CUtensorMap tm_d,
                 const __grid_constant__ CUtensorMap tm_f, const __grid_constant__ StepArgs a) {
   using T = Tile<K, TX, TY, F16, STAGES, UNI>;
-  extern __shared__ unsigned char smem_raw[];
-  unsigned char* smem = reinterpret_cast<unsigned char*>(
-      (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~static_cast<uintptr_t>(127));
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char* smem = align_smem(smem_raw);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + T::OFF_BAR);
 
   const int tid = threadIdx.x;
@@ -668,9 +674,8 @@ __global__ void __launch_bounds__(kThreads, K >= 3 ? 3 : (UNI ? 4 : 5))
     batch_kernel(const BatchGrid* __restrict__ grids, const int* __restrict__ unit_base,
                  const int* __restrict__ hdr, int launch_idx) {
   using T = Tile<K, TX, TY, F16, 1, UNI>;
-  extern __shared__ unsigned char smem_raw[];
-  unsigned char* smem = reinterpret_cast<unsigned char*>(
-      (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~static_cast<uintptr_t>(127));
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char* smem = align_smem(smem_raw);
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + T::OFF_BAR);
   float* sb = reinterpret_cast<float*>(smem + T::ST_B);
   float* sd = reinterpret_cast<float*>(smem + T::ST_D);
@@ -780,9 +785,10 @@ struct VariantTable {
   int n = 0;
   std::mutex mu;
   VariantTable() {
-    // Entries 0..3 are the defaults for K = 1..4 (measured on 4096^2: one CTA
-    // per tile with a small shared-memory footprint beats persistent
-    // double-buffered CTAs, which hold fewer CTAs per SM).
+    // Entries 0..3 are the first tile choice for K = 1..4 in the separate
+    // layout (measured on 4096^2: one CTA per tile with a small shared-memory
+    // footprint beats persistent double-buffered CTAs, which hold fewer CTAs
+    // per SM); step_variant_for names the default per K.
     add<1, 32, 32, 1>();  // 0  plain
     add<2, 64, 16, 1>();  // 1
     add<3, 64, 32, 1>();  // 2
@@ -853,8 +859,15 @@ int step_variant_count() { return table().n; }
 const StepVariant& step_variant(int i) { return table().e[i].v; }
 
 int step_variant_for(int k, int /*flux_storage*/) {
-  // Default tile per temporal depth: entries 0..3 of the table.
-  return (k >= 1 && k <= 4) ? k - 1 : -1;
+  // Default variant per temporal depth (fastest per depth on 4096^2): the
+  // plain 32x32 kernel for K = 1, the unified-layout 32x32 tiles for K > 1.
+  switch (k) {
+    case 1: return 0;
+    case 2: return 16;
+    case 3: return 18;
+    case 4: return 20;
+    default: return -1;
+  }
 }
 
 cudaError_t encode_step_maps(int variant, int flux_storage, int W, int H, int pitch,

@@ -612,6 +612,17 @@ def run_c3(args):
     batch = tws.Batch()
     for g in grids:
         batch.add(g)
+    # every batched variant on the same 192 steps (state reset before each)
+    sweep = {}
+    for vi, (k, tx, ty) in enumerate(tws.batch_variants()):
+        reset()
+        batch.set_variant(vi)
+        batch.step(32)
+        batch.sync()
+        t0 = time.perf_counter()
+        batch.step(192)
+        batch.sync()
+        sweep[f"{vi}_k{k}_{tx}x{ty}"] = round(cells * 192 / (time.perf_counter() - t0) / 1e9, 3)
     tuned = batch.autotune(32)
     batch.step(32)
     batch.sync()
@@ -655,6 +666,7 @@ def run_c3(args):
         "speedup_vs_one_grid_at_a_time": round(plain_s / batch_s, 3),
         "speedup_vs_concurrent_streams": round(plain_streams_s / batch_s, 3),
         "batched_variant": {"index": tuned, "k_tile": tws.batch_variants()[tuned]},
+        "batched_variant_sweep_gcell_steps_per_s": sweep,
         "chains": chains, "graph_replays": replayed,
         "fp64_checks": checks,
     }

@@ -698,7 +698,7 @@ struct tws_batch {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   std::vector<tws_grid*> grids;
-  int variant = 0;  // batched kernel variant
+  int variant = batch_variant_default();  // batched kernel variant
   bool use_graphs = true;
   int cap = 0;  // table capacity (grids)
   BatchGrid* d_grids = nullptr;
@@ -713,7 +713,7 @@ struct tws_batch {
   int uploaded_slot = -1;  // staging slot whose contents the device table holds
   int uploaded_m = 0;
   struct Graph {
-    int variant, launches;
+    int variant, launches, blocks;
     cudaGraphExec_t exec;
   };
   std::vector<Graph> graphs;
@@ -783,23 +783,31 @@ int ensure_capacity(tws_batch* b, int n) {
   return TWS_OK;
 }
 
-int run_launches(tws_batch* b, int variant, int launches) {
+int run_launches(tws_batch* b, int variant, int launches, int blocks) {
   for (int i = 0; i < launches; ++i) {
     cudaError_t e = launch_batch_step(variant, b->flux_storage, b->d_grids, b->d_base, b->d_hdr, i,
-                                      b->stream);
+                                      blocks, b->stream);
     if (e != cudaSuccess) return bfail(b, TWS_ERR_CUDA, std::string("batch launch: ") + cudaGetErrorString(e));
   }
   return TWS_OK;
 }
 
-cudaGraphExec_t graph_for(tws_batch* b, int variant, int launches) {
+// CTAs per launch for a chain of `units` tiles: the next power of two (at
+// least 256), so that graphs stay reusable while the membership changes.
+int launch_blocks(int units) {
+  int n = 256;
+  while (n < units) n *= 2;
+  return n;
+}
+
+cudaGraphExec_t graph_for(tws_batch* b, int variant, int launches, int blocks) {
   for (auto& gr : b->graphs)
-    if (gr.variant == variant && gr.launches == launches) return gr.exec;
+    if (gr.variant == variant && gr.launches == launches && gr.blocks == blocks) return gr.exec;
   if (prepare_batch_variant(variant, b->flux_storage) != cudaSuccess) return nullptr;
   cudaGraph_t graph = nullptr;
   if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
     return nullptr;
-  const int rc = run_launches(b, variant, launches);
+  const int rc = run_launches(b, variant, launches, blocks);
   const cudaError_t ee = cudaStreamEndCapture(b->stream, &graph);
   if (rc != TWS_OK || ee != cudaSuccess || !graph) {
     if (graph) cudaGraphDestroy(graph);
@@ -813,7 +821,11 @@ cudaGraphExec_t graph_for(tws_batch* b, int variant, int launches) {
     cudaGetLastError();
     return nullptr;
   }
-  b->graphs.push_back({variant, launches, exec});
+  if (b->graphs.size() >= 64) {  // bounded cache: drop the oldest graph
+    cudaGraphExecDestroy(b->graphs.front().exec);
+    b->graphs.erase(b->graphs.begin());
+  }
+  b->graphs.push_back({variant, launches, blocks, exec});
   return exec;
 }
 
@@ -880,14 +892,15 @@ int run_chain(tws_batch* b, int variant, const std::vector<int>& launches) {
     b->uploaded_slot = s;
     b->uploaded_m = m;
   }
-  cudaGraphExec_t exec = b->use_graphs ? graph_for(b, variant, max_l) : nullptr;
+  const int blocks = launch_blocks(units);
+  cudaGraphExec_t exec = b->use_graphs ? graph_for(b, variant, max_l, blocks) : nullptr;
   if (exec) {
     if (cudaGraphLaunch(exec, b->stream) != cudaSuccess)
       return bfail(b, TWS_ERR_CUDA, "graph launch failed");
     count_launch((uint64_t)max_l);
     ++b->graph_launches;
   } else {
-    rc = run_launches(b, variant, max_l);
+    rc = run_launches(b, variant, max_l, blocks);
     if (rc != TWS_OK) return rc;
   }
   ++b->chains;

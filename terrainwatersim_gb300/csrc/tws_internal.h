@@ -77,10 +77,13 @@ struct alignas(64) BatchGrid {
 // unit_base[ngrids] = total units.  Launch `launch_idx` of a chain advances
 // grid g iff launch_idx < grids[g].launches.
 int batch_variant_count();
+int batch_variant_default();  // two steps per launch, unified 32x32 tiles
 void batch_variant_info(int i, int* k, int* tx, int* ty, int* step_variant);
 cudaError_t prepare_batch_variant(int variant, int flux_storage);  // outside any capture
+// `blocks` >= the chain's total units (one CTA per unit; extra CTAs return).
 cudaError_t launch_batch_step(int variant, int flux_storage, const BatchGrid* grids,
-                              const int* unit_base, const int* hdr, int launch_idx, cudaStream_t s);
+                              const int* unit_base, const int* hdr, int launch_idx, int blocks,
+                              cudaStream_t s);
 
 // Device error codes written to StepArgs::err.
 enum : int { kDevErrNone = 0, kDevErrWaitTimeout = 1 };

@@ -388,7 +388,13 @@ __device__ __forceinline__ void ring_for(int tid, F&& body) {
 //
 // The cell arithmetic is process_tile's, with channel pairs in packed f32x2
 // operations, so results are identical.
-template <int K, int TX, int TY, bool F16, int STAGES>
+//
+// INTERIOR: the box lies inside the grid.  Otherwise (a tile at the grid's
+// edge) each visited cell finds its grid coordinates from p: cells off the
+// grid keep the zero flux, depth and surface the box loaded with (the
+// shaders' out-of-range reads), and closed walls zero the outflow across the
+// border, as in process_tile.
+template <int K, int TX, int TY, bool F16, int STAGES, bool INTERIOR>
 __device__ __forceinline__ void process_tile_flat(const StepArgs& a, float* __restrict__ d_out,
                                                   void* __restrict__ f_out,
                                                   float2* __restrict__ v_out, int x0, int y0,
@@ -402,6 +408,15 @@ __device__ __forceinline__ void process_tile_flat(const StepArgs& a, float* __re
   const float fscale = a.flux_scale, finv = a.flux_inv_scale;
   const float2 kf2 = make_float2(kf, kf), ka2 = make_float2(ka, ka);
   const float2 fscale2 = make_float2(fscale, fscale), finv2 = make_float2(finv, finv);
+  const int W = a.W, H = a.H;
+  const bool closed = a.closed != 0;
+  // grid coordinates of box cell p, and whether it is on the grid
+  auto cell = [&](int p, int& gx, int& gy) {
+    const int r = p / S;
+    gx = x0 - T::HX + (p - r * S);
+    gy = y0 - T::HY + r;
+    return INTERIOR || (gx >= 0 && gx < W && gy >= 0 && gy < H);
+  };
   float* const planes = reinterpret_cast<float*>(fbox);
   float* __restrict__ fx = planes;
   float* __restrict__ fy = planes + T::NB;
@@ -414,9 +429,12 @@ __device__ __forceinline__ void process_tile_flat(const StepArgs& a, float* __re
   // Phase 0: first step's sources and h = d + b (flowUpdate.comp:34).
   if (mask) {
     ring_for<0, T::NB - 1>(tid, [&](int p) {
-      const int r = p / S;
-      const float d = add_sources(sd[p], x0 - T::HX + (p - r * S), y0 - T::HY + r, a, mask);
-      sd[p] = d;
+      int gx, gy;
+      float d = sd[p];
+      if (cell(p, gx, gy)) {
+        d = add_sources(d, gx, gy, a, mask);
+        sd[p] = d;
+      }
       sh[p] = fadd(d, sb[p]);
     });
   } else {
@@ -428,6 +446,8 @@ __device__ __forceinline__ void process_tile_flat(const StepArgs& a, float* __re
   // Channel pairs (+x, -x) and (+y, -y) go through the packed f32x2 ops.
   auto outflow = [&](int p, auto s_) -> float4 {
     constexpr int s = decltype(s_)::value;
+    int gx = 0, gy = 0;
+    if (!cell(p, gx, gy)) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // stays zero
     float4 fo;
     if constexpr (s > 0) {
       fo = make_float4(fx[p], fy[p], fz[p], fw[p]);
@@ -450,6 +470,12 @@ __device__ __forceinline__ void process_tile_flat(const StepArgs& a, float* __re
     const float2 py = fmul2(make_float2(fo.z, fo.w), kf2), qy = fmul2(ey, ka2);
     float2 nx = make_float2(max0_fast(fadd(px.x, qx.x)), max0_fast(fadd(px.y, qx.y)));
     float2 ny = make_float2(max0_fast(fadd(py.x, qy.x)), max0_fast(fadd(py.y, qy.y)));
+    if (!INTERIOR && closed) {  // no outflow across a closed wall
+      if (gx + 1 >= W) nx.x = 0.0f;
+      if (gx == 0) nx.y = 0.0f;
+      if (gy + 1 >= H) ny.x = 0.0f;
+      if (gy == 0) ny.y = 0.0f;
+    }
     const float total = fmul(fadd(fadd(fadd(nx.x, nx.y), ny.x), ny.y), cc);
     if (total > dc) {
       const float sc = scale_factor(dc, total);
@@ -480,13 +506,14 @@ __device__ __forceinline__ void process_tile_flat(const StepArgs& a, float* __re
   // Phase B: depth update, flowApply.comp:32-52, then the next step's sources
   // and surface height.
   auto depth = [&](int p) {
+    int gx = 0, gy = 0;
+    if (!INTERIOR || mask) {
+      if (!cell(p, gx, gy)) return;  // off the grid: depth and surface stay zero
+    }
     const float4 fc = make_float4(fx[p], fy[p], fz[p], fw[p]);
     const float2 io = in_out(p, fc);
     float dn = max0_fast(fadd(sd[p], fmul(fsub(io.x, io.y), cc)));
-    if (mask) {
-      const int r = p / S;
-      dn = add_sources(dn, x0 - T::HX + (p - r * S), y0 - T::HY + r, a, mask);
-    }
+    if (mask) dn = add_sources(dn, gx, gy, a, mask);
     sd[p] = dn;
     sh[p] = fadd(dn, sb[p]);
   };
@@ -498,6 +525,7 @@ __device__ __forceinline__ void process_tile_flat(const StepArgs& a, float* __re
     for (int it = 0; it < TX * TY / kThreads; ++it) {
       const int idx = it * kThreads + tid;
       const int i = idx / TX, j = idx % TX;
+      if (!INTERIOR && (x0 + j >= W || y0 + i >= H)) continue;  // past the grid's edge
       const int p = (T::HY + i) * S + T::HX + j;
       const float4 fc = make_float4(fx[p], fy[p], fz[p], fw[p]);
       const float X1 = fy[p + 1];  // -x outflow of the +x neighbour
@@ -629,13 +657,18 @@ __global__ void __launch_bounds__(kThreads)
     const bool ok = wait_bounded(&bars[s], parity, a.err, a.wait_cycles);
     if (__syncthreads_or(!ok)) return;  // every thread leaves together on a time-out
 
-    if (x0 - T::HX >= 0 && y0 - T::HY >= 0 && x0 + TX + T::HX <= a.W && y0 + TY + T::HY <= a.H) {
-      if constexpr (UNI)
-        process_tile_flat<K, TX, TY, F16, STAGES>(a, a.d_out, a.f_out, a.v_out, x0, y0, mask, sb,
-                                                  sd, sh, st + T::ST_F);
+    const bool interior =
+        x0 - T::HX >= 0 && y0 - T::HY >= 0 && x0 + TX + T::HX <= a.W && y0 + TY + T::HY <= a.H;
+    if constexpr (UNI) {
+      if (interior)
+        process_tile_flat<K, TX, TY, F16, STAGES, true>(a, a.d_out, a.f_out, a.v_out, x0, y0,
+                                                        mask, sb, sd, sh, st + T::ST_F);
       else
-        process_tile<K, TX, TY, F16, STAGES, UNI, true>(a, a.d_out, a.f_out, a.v_out, x0, y0,
-                                                        mask, sb, sd, sh, sf, st + T::ST_F);
+        process_tile_flat<K, TX, TY, F16, STAGES, false>(a, a.d_out, a.f_out, a.v_out, x0, y0,
+                                                         mask, sb, sd, sh, st + T::ST_F);
+    } else if (interior) {
+      process_tile<K, TX, TY, F16, STAGES, UNI, true>(a, a.d_out, a.f_out, a.v_out, x0, y0, mask,
+                                                      sb, sd, sh, sf, st + T::ST_F);
     } else {
       process_tile<K, TX, TY, F16, STAGES, UNI, false>(a, a.d_out, a.f_out, a.v_out, x0, y0, mask,
                                                        sb, sd, sh, sf, st + T::ST_F);
@@ -664,16 +697,31 @@ __device__ __forceinline__ void tensormap_acquire(const void* tm) {
 }
 
 // Many grids of different sizes advance in one launch.  Work units are the
-// tiles of every member grid, numbered grid by grid (unit_base); persistent
-// CTAs stride through them, find their grid by binary search, load the tile
-// through that grid's tensor maps and run the same per-tile steps as
-// step_kernel.  Launch `launch_idx` of a chain skips grids that have taken
-// all their launches, so grids with different step counts share a chain.
-template <int K, int TX, int TY, bool F16, bool UNI>
-__global__ void __launch_bounds__(kThreads, K >= 3 ? 3 : (UNI ? 4 : 5))
+// tiles of every member grid, numbered grid by grid (unit_base); CTA u takes
+// unit u, finds its grid by binary search, loads the tile through that
+// grid's tensor maps and runs the same per-tile steps as step_kernel.  One
+// CTA per unit (the launch has at least as many CTAs as units; the rest
+// return at once): a persistent loop over units would keep its state live
+// across the tile and push the tile code into register spills.  Launch
+// `launch_idx` of a chain skips grids that have taken all their launches, so
+// grids with different step counts share a chain.
+template <int K, int TX, int TY, bool F16, bool UNI, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB)
     batch_kernel(const BatchGrid* __restrict__ grids, const int* __restrict__ unit_base,
                  const int* __restrict__ hdr, int launch_idx) {
   using T = Tile<K, TX, TY, F16, 1, UNI>;
+  const int ngrids = hdr[0];
+  const int u = blockIdx.x;
+  if (u >= __ldg(unit_base + ngrids)) return;
+  int lo = 0, hi = ngrids - 1;  // last grid whose first unit is <= u
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(unit_base + mid) <= u) lo = mid;
+    else hi = mid - 1;
+  }
+  const BatchGrid& G = grids[lo];
+  if (launch_idx >= G.launches) return;
+
   extern __shared__ __align__(128) unsigned char smem_raw[];
   unsigned char* smem = align_smem(smem_raw);
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + T::OFF_BAR);
@@ -683,62 +731,48 @@ __global__ void __launch_bounds__(kThreads, K >= 3 ? 3 : (UNI ? 4 : 5))
   float4* sf = (F16 && !UNI) ? reinterpret_cast<float4*>(smem + T::OFF_WORK)
                              : reinterpret_cast<float4*>(smem + T::ST_F);
   const int tid = threadIdx.x;
-  const int ngrids = hdr[0];
-  const int total = unit_base[ngrids];
+  const int t = u - __ldg(unit_base + lo);
+  const int x0 = (t % G.tiles_x) * TX, y0 = (t / G.tiles_x) * TY;
+  const int p = (G.cur + launch_idx) & 1;
+  const StepArgs& a = G.a;
 
   if (tid == 0) {
     mbar_init(bar, 1);
     fence_mbar_init();
+    tensormap_acquire(&G.tm_b);
+    tensormap_acquire(&G.tm_d[p]);
+    tensormap_acquire(&G.tm_f[p]);
+    issue_tile<T, F16>(smem, bar, &G.tm_b, &G.tm_d[p], &G.tm_f[p], x0, y0, a.missing_tx);
   }
-  __syncthreads();
-
-  uint32_t it = 0;
-  for (int u = blockIdx.x; u < total; u += gridDim.x) {
-    int lo = 0, hi = ngrids - 1;  // last grid whose first unit is <= u
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (__ldg(unit_base + mid) <= u) lo = mid;
-      else hi = mid - 1;
-    }
-    const BatchGrid& G = grids[lo];
-    if (launch_idx >= G.launches) continue;
-    const int t = u - __ldg(unit_base + lo);
-    const int x0 = (t % G.tiles_x) * TX, y0 = (t / G.tiles_x) * TY;
-    const int p = (G.cur + launch_idx) & 1;
-    const StepArgs& a = G.a;
-
-    if (tid == 0) {
-      tensormap_acquire(&G.tm_b);
-      tensormap_acquire(&G.tm_d[p]);
-      tensormap_acquire(&G.tm_f[p]);
-      issue_tile<T, F16>(smem, bar, &G.tm_b, &G.tm_d[p], &G.tm_f[p], x0, y0, a.missing_tx);
-    }
-    uint32_t mask = 0;
+  uint32_t mask = 0;
 #pragma unroll
-    for (int k = 0; k < TWS_MAX_SOURCES; ++k) {
-      if (k < a.nsrc) {
-        const DevSource& src = a.src[k];
-        if (src.bx1 >= x0 - T::HX && src.bx0 < x0 + TX + T::HX && src.by1 >= y0 - T::HY &&
-            src.by0 < y0 + TY + T::HY)
-          mask |= 1u << k;
-      }
+  for (int k = 0; k < TWS_MAX_SOURCES; ++k) {
+    if (k < a.nsrc) {
+      const DevSource& src = a.src[k];
+      if (src.bx1 >= x0 - T::HX && src.bx0 < x0 + TX + T::HX && src.by1 >= y0 - T::HY &&
+          src.by0 < y0 + TY + T::HY)
+        mask |= 1u << k;
     }
-    const bool ok = wait_bounded(bar, it & 1u, a.err, a.wait_cycles);
-    ++it;
-    if (__syncthreads_or(!ok)) return;
-    const int gw = a.W, gh = a.H;
-    if (x0 - T::HX >= 0 && y0 - T::HY >= 0 && x0 + TX + T::HX <= gw && y0 + TY + T::HY <= gh) {
-      if constexpr (UNI)
-        process_tile_flat<K, TX, TY, F16, 1>(a, G.d[p ^ 1], G.f[p ^ 1], G.v, x0, y0, mask, sb, sd,
-                                             sh, smem + T::ST_F);
-      else
-        process_tile<K, TX, TY, F16, 1, UNI, true>(a, G.d[p ^ 1], G.f[p ^ 1], G.v, x0, y0, mask,
-                                                   sb, sd, sh, sf, smem + T::ST_F);
-    } else {
-      process_tile<K, TX, TY, F16, 1, UNI, false>(a, G.d[p ^ 1], G.f[p ^ 1], G.v, x0, y0, mask, sb,
-                                                  sd, sh, sf, smem + T::ST_F);
-    }
-    __syncthreads();  // the tile buffers are free again
+  }
+  __syncthreads();  // the barrier is initialised before anyone waits on it
+  const bool ok = wait_bounded(bar, 0, a.err, a.wait_cycles);
+  if (__syncthreads_or(!ok)) return;
+  const int gw = a.W, gh = a.H;
+  const bool interior =
+      x0 - T::HX >= 0 && y0 - T::HY >= 0 && x0 + TX + T::HX <= gw && y0 + TY + T::HY <= gh;
+  if constexpr (UNI) {
+    if (interior)
+      process_tile_flat<K, TX, TY, F16, 1, true>(a, G.d[p ^ 1], G.f[p ^ 1], G.v, x0, y0, mask, sb,
+                                                 sd, sh, smem + T::ST_F);
+    else
+      process_tile_flat<K, TX, TY, F16, 1, false>(a, G.d[p ^ 1], G.f[p ^ 1], G.v, x0, y0, mask,
+                                                  sb, sd, sh, smem + T::ST_F);
+  } else if (interior) {
+    process_tile<K, TX, TY, F16, 1, UNI, true>(a, G.d[p ^ 1], G.f[p ^ 1], G.v, x0, y0, mask, sb,
+                                               sd, sh, sf, smem + T::ST_F);
+  } else {
+    process_tile<K, TX, TY, F16, 1, UNI, false>(a, G.d[p ^ 1], G.f[p ^ 1], G.v, x0, y0, mask, sb,
+                                                sd, sh, sf, smem + T::ST_F);
   }
 }
 
@@ -988,7 +1022,10 @@ struct BatchEntry {
   bool set[2] = {false, false};
 };
 
-template <int K, int TX, int TY, bool UNI>
+// MINB: CTAs per SM the register allocation must allow (the batched kernel
+// keeps its grid's scalars in registers, where the single-grid kernel reads
+// them from the parameter bank).
+template <int K, int TX, int TY, bool UNI, int MINB>
 BatchEntry make_batch_entry(int step_variant) {
   BatchEntry e;
   e.k = K;
@@ -996,25 +1033,27 @@ BatchEntry make_batch_entry(int step_variant) {
   e.ty = TY;
   e.uni = UNI;
   e.step_variant = step_variant;
-  e.fn[TWS_FLUX_F32] = reinterpret_cast<const void*>(&batch_kernel<K, TX, TY, false, UNI>);
-  e.fn[TWS_FLUX_F16] = reinterpret_cast<const void*>(&batch_kernel<K, TX, TY, true, UNI>);
+  e.fn[TWS_FLUX_F32] = reinterpret_cast<const void*>(&batch_kernel<K, TX, TY, false, UNI, MINB>);
+  e.fn[TWS_FLUX_F16] = reinterpret_cast<const void*>(&batch_kernel<K, TX, TY, true, UNI, MINB>);
   e.smem[TWS_FLUX_F32] = Tile<K, TX, TY, false, 1, UNI>::SMEM;
   e.smem[TWS_FLUX_F16] = Tile<K, TX, TY, true, 1, UNI>::SMEM;
   return e;
 }
 
 struct BatchTable {
-  BatchEntry e[8];
+  BatchEntry e[12];
   int n = 0;
   std::mutex mu;
   BatchTable() {
-    e[n++] = make_batch_entry<1, 32, 32, false>(0);
-    e[n++] = make_batch_entry<2, 32, 32, false>(10);
-    e[n++] = make_batch_entry<1, 64, 16, false>(4);
-    e[n++] = make_batch_entry<2, 64, 16, false>(1);
-    e[n++] = make_batch_entry<2, 32, 32, true>(16);
-    e[n++] = make_batch_entry<2, 64, 16, true>(17);
-    e[n++] = make_batch_entry<3, 32, 32, true>(18);
+    e[n++] = make_batch_entry<1, 32, 32, false, 5>(0);
+    e[n++] = make_batch_entry<2, 32, 32, false, 5>(10);
+    e[n++] = make_batch_entry<1, 64, 16, false, 5>(4);
+    e[n++] = make_batch_entry<2, 64, 16, false, 5>(1);
+    e[n++] = make_batch_entry<2, 32, 32, true, 4>(16);
+    e[n++] = make_batch_entry<2, 64, 16, true, 4>(17);
+    e[n++] = make_batch_entry<3, 32, 32, true, 3>(18);
+    e[n++] = make_batch_entry<2, 32, 32, true, 3>(16);
+    e[n++] = make_batch_entry<2, 32, 32, true, 5>(16);
   }
 };
 
@@ -1026,6 +1065,7 @@ BatchTable& batch_table() {
 }  // namespace
 
 int batch_variant_count() { return batch_table().n; }
+int batch_variant_default() { return 4; }
 
 void batch_variant_info(int i, int* k, int* tx, int* ty, int* step_variant) {
   const BatchEntry& e = batch_table().e[i];
@@ -1058,22 +1098,15 @@ cudaError_t prepare_batch_variant(int variant, int flux_storage) {
 }
 
 cudaError_t launch_batch_step(int variant, int flux_storage, const BatchGrid* grids,
-                              const int* unit_base, const int* hdr, int launch_idx,
+                              const int* unit_base, const int* hdr, int launch_idx, int blocks,
                               cudaStream_t s) {
   cudaError_t err = prepare_batch_variant(variant, flux_storage);
   if (err != cudaSuccess) return err;
+  if (blocks <= 0) return cudaErrorInvalidValue;
   const int fs = flux_storage == TWS_FLUX_F16 ? TWS_FLUX_F16 : TWS_FLUX_F32;
   BatchEntry& e = batch_table().e[variant];
-  const int ctas = e.ctas_per_sm[fs];
-  static int sms = 0;
-  if (sms == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
-  }
   auto fn = reinterpret_cast<BatchFn>(const_cast<void*>(e.fn[fs]));
-  fn<<<sms * ctas, kThreads, e.smem[fs], s>>>(grids, unit_base, hdr, launch_idx);
+  fn<<<blocks, kThreads, e.smem[fs], s>>>(grids, unit_base, hdr, launch_idx);
   count_launch();
   return cudaGetLastError();
 }

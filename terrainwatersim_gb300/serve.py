@@ -72,11 +72,11 @@ def make_request(rid, width, height, seed, fill, params, sources, steps, arrival
 
 class Server:
     def __init__(self, memory_budget_bytes=120e9, flux_storage=FLUX_F16, chain_steps=0,
-                 batch_variant=1, keep_grids=False):
+                 batch_variant=4, keep_grids=False):
         """chain_steps <= 0 sizes each chain to about 1.5e9 cell-steps.
-        batch_variant: the batched kernel (default 1: two steps per launch on
-        32x32 tiles, the fastest on every measured mix); -1 autotunes on the
-        first chain."""
+        batch_variant: the batched kernel (default 4: two steps per launch on
+        unified-layout 32x32 tiles, the library's default); -1 autotunes on
+        the first chain."""
         self.cfg = ServerConfig(memory_budget_bytes, flux_storage, chain_steps, batch_variant,
                                 1 if keep_grids else 0)
         h = C.c_void_p()

@@ -700,18 +700,18 @@ struct tws_batch {
   std::vector<tws_grid*> grids;
   int variant = batch_variant_default();  // batched kernel variant
   bool use_graphs = true;
-  int cap = 0;  // table capacity (grids)
+  int cap = 0;   // table capacity (grids)
+  int ucap = 0;  // unit table capacity
   BatchGrid* d_grids = nullptr;
-  int* d_base = nullptr;
-  int* d_hdr = nullptr;
+  BatchUnit* d_units = nullptr;
   // host staging, two slots so that filling one does not wait for the copy of the other
   BatchGrid* h_grids[2] = {nullptr, nullptr};
-  int* h_base[2] = {nullptr, nullptr};
-  int* h_hdr[2] = {nullptr, nullptr};
+  BatchUnit* h_units[2] = {nullptr, nullptr};
   cudaEvent_t copied[2] = {nullptr, nullptr};
   int slot = 0;
   int uploaded_slot = -1;  // staging slot whose contents the device table holds
   int uploaded_m = 0;
+  int uploaded_blocks = 0;
   struct Graph {
     int variant, launches, blocks;
     cudaGraphExec_t exec;
@@ -735,23 +735,26 @@ void drop_graphs(tws_batch* b) {
   b->graphs.clear();
 }
 
+void free_units(tws_batch* b) {
+  cudaFree(b->d_units);
+  for (int s = 0; s < 2; ++s) {
+    if (b->h_units[s]) cudaFreeHost(b->h_units[s]);
+    b->h_units[s] = nullptr;
+  }
+  b->d_units = nullptr;
+  b->ucap = 0;
+  b->uploaded_slot = -1;  // the device table is gone
+}
+
 void free_table(tws_batch* b) {
   cudaFree(b->d_grids);
-  cudaFree(b->d_base);
-  cudaFree(b->d_hdr);
   for (int s = 0; s < 2; ++s) {
     if (b->h_grids[s]) cudaFreeHost(b->h_grids[s]);
-    if (b->h_base[s]) cudaFreeHost(b->h_base[s]);
-    if (b->h_hdr[s]) cudaFreeHost(b->h_hdr[s]);
     b->h_grids[s] = nullptr;
-    b->h_base[s] = nullptr;
-    b->h_hdr[s] = nullptr;
   }
   b->d_grids = nullptr;
-  b->d_base = nullptr;
-  b->d_hdr = nullptr;
   b->cap = 0;
-  b->uploaded_slot = -1;  // the device table is gone
+  free_units(b);
 }
 
 // Grow the table to hold n grids (graphs reference the device arrays, so they
@@ -763,17 +766,13 @@ int ensure_capacity(tws_batch* b, int n) {
   free_table(b);
   int cap = 16;
   while (cap < n) cap *= 2;
-  if (cudaMalloc(&b->d_grids, sizeof(BatchGrid) * cap) != cudaSuccess ||
-      cudaMalloc(&b->d_base, sizeof(int) * (cap + 1)) != cudaSuccess ||
-      cudaMalloc(&b->d_hdr, sizeof(int) * 4) != cudaSuccess) {
+  if (cudaMalloc(&b->d_grids, sizeof(BatchGrid) * cap) != cudaSuccess) {
     cudaGetLastError();
     free_table(b);
     return bfail(b, TWS_ERR_OOM, "batch table allocation failed");
   }
   for (int s = 0; s < 2; ++s) {
-    if (cudaMallocHost(&b->h_grids[s], sizeof(BatchGrid) * cap) != cudaSuccess ||
-        cudaMallocHost(&b->h_base[s], sizeof(int) * (cap + 1)) != cudaSuccess ||
-        cudaMallocHost(&b->h_hdr[s], sizeof(int) * 4) != cudaSuccess) {
+    if (cudaMallocHost(&b->h_grids[s], sizeof(BatchGrid) * cap) != cudaSuccess) {
       cudaGetLastError();
       free_table(b);
       return bfail(b, TWS_ERR_OOM, "batch staging allocation failed");
@@ -783,10 +782,32 @@ int ensure_capacity(tws_batch* b, int n) {
   return TWS_OK;
 }
 
+// Grow the unit table to n entries (n is a launch's CTA count, a power of two).
+int ensure_units(tws_batch* b, int n) {
+  if (n <= b->ucap) return TWS_OK;
+  cudaStreamSynchronize(b->stream);
+  drop_graphs(b);
+  free_units(b);
+  if (cudaMalloc(&b->d_units, sizeof(BatchUnit) * n) != cudaSuccess) {
+    cudaGetLastError();
+    free_units(b);
+    return bfail(b, TWS_ERR_OOM, "batch unit table allocation failed");
+  }
+  for (int s = 0; s < 2; ++s) {
+    if (cudaMallocHost(&b->h_units[s], sizeof(BatchUnit) * n) != cudaSuccess) {
+      cudaGetLastError();
+      free_units(b);
+      return bfail(b, TWS_ERR_OOM, "batch unit staging allocation failed");
+    }
+  }
+  b->ucap = n;
+  return TWS_OK;
+}
+
 int run_launches(tws_batch* b, int variant, int launches, int blocks) {
   for (int i = 0; i < launches; ++i) {
-    cudaError_t e = launch_batch_step(variant, b->flux_storage, b->d_grids, b->d_base, b->d_hdr, i,
-                                      blocks, b->stream);
+    cudaError_t e =
+        launch_batch_step(variant, b->flux_storage, b->d_grids, b->d_units, i, blocks, b->stream);
     if (e != cudaSuccess) return bfail(b, TWS_ERR_CUDA, std::string("batch launch: ") + cudaGetErrorString(e));
   }
   return TWS_OK;
@@ -836,14 +857,27 @@ int run_chain(tws_batch* b, int variant, const std::vector<int>& launches) {
   const int n = (int)b->grids.size();
   int rc = ensure_capacity(b, n);
   if (rc != TWS_OK) return rc;
+  int units = 0, m = 0, max_l = 0;
+  for (int i = 0; i < n; ++i) {
+    if (launches[i] <= 0) continue;
+    const tws_grid* g = b->grids[i];
+    units += ((g->W + tx - 1) / tx) * ((g->H + ty - 1) / ty);
+    max_l = std::max(max_l, launches[i]);
+    ++m;
+  }
+  if (m == 0) return TWS_OK;
+  const int blocks = launch_blocks(units);
+  rc = ensure_units(b, blocks);
+  if (rc != TWS_OK) return rc;
   // wait until the copy that last read this staging slot has completed
   const int s = b->slot;
   b->slot ^= 1;
   if (b->copied[s]) cudaEventSynchronize(b->copied[s]);
   BatchGrid* hg = b->h_grids[s];
-  int* hb = b->h_base[s];
-  int m = 0, units = 0, max_l = 0;
+  BatchUnit* hu = b->h_units[s];
   std::string why;
+  m = 0;
+  int u = 0;
   for (int i = 0; i < n; ++i) {
     if (launches[i] <= 0) continue;
     tws_grid* g = b->grids[i];
@@ -866,33 +900,31 @@ int run_chain(tws_batch* b, int variant, const std::vector<int>& launches) {
     e.cur = g->cur;
     e.launches = launches[i];
     e.tiles_x = (g->W + tx - 1) / tx;
-    hb[m] = units;
-    units += e.tiles_x * ((g->H + ty - 1) / ty);
-    max_l = std::max(max_l, launches[i]);
+    const int meta = launches[i] | (g->cur << 30);
+    for (int y0 = 0; y0 < g->H; y0 += ty)
+      for (int x0 = 0; x0 < g->W; x0 += tx) hu[u++] = BatchUnit{m, x0, y0, meta};
     ++m;
   }
-  if (m == 0) return TWS_OK;
-  hb[m] = units;
-  b->h_hdr[s][0] = m;
+  for (; u < blocks; ++u) hu[u] = BatchUnit{0, 0, 0, 0};  // CTAs past the units return
   // Upload the table unless it equals the one the device already holds (the
   // same members, launch counts and parity: consecutive chains of a steady
-  // batch with an even number of launches).
+  // batch with an even number of launches).  The units follow from the
+  // members and the launch size.
   const int prev = b->uploaded_slot;
-  const bool same = prev >= 0 && b->uploaded_m == m &&
-                    std::memcmp(hg, b->h_grids[prev], sizeof(BatchGrid) * m) == 0 &&
-                    std::memcmp(hb, b->h_base[prev], sizeof(int) * (m + 1)) == 0;
+  const bool same = prev >= 0 && b->uploaded_m == m && b->uploaded_blocks == blocks &&
+                    std::memcmp(hg, b->h_grids[prev], sizeof(BatchGrid) * m) == 0;
   if (same) {
     b->slot = prev ^ 1;  // keep the uploaded copy in its slot for the next comparison
   } else {
     cudaMemcpyAsync(b->d_grids, hg, sizeof(BatchGrid) * m, cudaMemcpyHostToDevice, b->stream);
-    cudaMemcpyAsync(b->d_base, hb, sizeof(int) * (m + 1), cudaMemcpyHostToDevice, b->stream);
-    cudaMemcpyAsync(b->d_hdr, b->h_hdr[s], sizeof(int) * 4, cudaMemcpyHostToDevice, b->stream);
+    cudaMemcpyAsync(b->d_units, hu, sizeof(BatchUnit) * blocks, cudaMemcpyHostToDevice,
+                    b->stream);
     if (!b->copied[s]) cudaEventCreateWithFlags(&b->copied[s], cudaEventDisableTiming);
     cudaEventRecord(b->copied[s], b->stream);
     b->uploaded_slot = s;
     b->uploaded_m = m;
+    b->uploaded_blocks = blocks;
   }
-  const int blocks = launch_blocks(units);
   cudaGraphExec_t exec = b->use_graphs ? graph_for(b, variant, max_l, blocks) : nullptr;
   if (exec) {
     if (cudaGraphLaunch(exec, b->stream) != cudaSuccess)

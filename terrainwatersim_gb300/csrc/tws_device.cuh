@@ -57,8 +57,11 @@ __device__ __forceinline__ float saturate01(float v) {
 }
 
 // ---- the source term -----------------------------------------------------------
-__device__ __forceinline__ float add_sources(float d, int gx, int gy, const StepArgs& a,
-                                             uint32_t mask) {
+// Not inlined: only tiles that a source touches call it, and an inlined copy
+// in every unrolled cell loop of the tile kernels would multiply their code
+// size past the instruction cache.
+static __device__ __noinline__ float add_sources(float d, int gx, int gy, const StepArgs& a,
+                                                 uint32_t mask) {
 #pragma unroll
   for (int k = 0; k < TWS_MAX_SOURCES; ++k) {
     if (!((mask >> k) & 1u)) continue;

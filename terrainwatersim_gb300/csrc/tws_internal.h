@@ -72,18 +72,23 @@ struct alignas(64) BatchGrid {
   int pad_;
 };
 
-// Batched kernel variants (K steps per launch, tile) and their launcher:
-// `hdr` = {number of grids}, `unit_base[g]` = first work unit (tile) of grid g,
-// unit_base[ngrids] = total units.  Launch `launch_idx` of a chain advances
-// grid g iff launch_idx < grids[g].launches.
+// One work unit (tile) of a batched launch, as the batched kernel reads it:
+// its grid (index into the BatchGrid table), tile origin, and meta =
+// launches this chain gives the grid | (the grid's buffer parity at the chain
+// start) << 30.  Entries past the chain's units have meta = 0.
+struct BatchUnit {
+  int grid, x0, y0, meta;
+};
+
+// Batched kernel variants (K steps per launch, tile) and their launcher.
+// Launch `launch_idx` of a chain runs CTA u on units[u] (`blocks` CTAs, at
+// least the chain's units) and advances a grid iff launch_idx < its launches.
 int batch_variant_count();
 int batch_variant_default();  // two steps per launch, unified 32x32 tiles
 void batch_variant_info(int i, int* k, int* tx, int* ty, int* step_variant);
 cudaError_t prepare_batch_variant(int variant, int flux_storage);  // outside any capture
-// `blocks` >= the chain's total units (one CTA per unit; extra CTAs return).
 cudaError_t launch_batch_step(int variant, int flux_storage, const BatchGrid* grids,
-                              const int* unit_base, const int* hdr, int launch_idx, int blocks,
-                              cudaStream_t s);
+                              const BatchUnit* units, int launch_idx, int blocks, cudaStream_t s);
 
 // Device error codes written to StepArgs::err.
 enum : int { kDevErrNone = 0, kDevErrWaitTimeout = 1 };

@@ -359,13 +359,20 @@ __device__ __forceinline__ void process_tile(const StepArgs& a, float* __restric
 // Runs body(p) for p = FIRST .. LAST, thread tid taking FIRST + tid,
 // FIRST + tid + kThreads, ...: fully unrolled, so every position's shared
 // memory address is a constant offset from one register.
-template <int FIRST, int LAST, class F>
+// UNROLL = false: an ordinary loop instead (tiles at the grid's edge, which
+// are few: their code stays small and out of the instruction cache's way).
+template <int FIRST, int LAST, bool UNROLL, class F>
 __device__ __forceinline__ void ring_for(int tid, F&& body) {
-  constexpr int N = LAST - FIRST + 1;
-  constexpr int FULL = N / kThreads, REM = N % kThreads;
+  if constexpr (UNROLL) {
+    constexpr int N = LAST - FIRST + 1;
+    constexpr int FULL = N / kThreads, REM = N % kThreads;
 #pragma unroll
-  for (int it = 0; it < FULL; ++it) body(FIRST + it * kThreads + tid);
-  if (REM > 0 && tid < REM) body(FIRST + FULL * kThreads + tid);
+    for (int it = 0; it < FULL; ++it) body(FIRST + it * kThreads + tid);
+    if (REM > 0 && tid < REM) body(FIRST + FULL * kThreads + tid);
+  } else {
+#pragma unroll 1
+    for (int p = FIRST + tid; p <= LAST; p += kThreads) body(p);
+  }
 }
 
 // K steps of an interior tile in the unified layout: b, d, h and f share the
@@ -428,7 +435,7 @@ __device__ __forceinline__ void process_tile_flat(const StepArgs& a, float* __re
 
   // Phase 0: first step's sources and h = d + b (flowUpdate.comp:34).
   if (mask) {
-    ring_for<0, T::NB - 1>(tid, [&](int p) {
+    ring_for<0, T::NB - 1, INTERIOR>(tid, [&](int p) {
       int gx, gy;
       float d = sd[p];
       if (cell(p, gx, gy)) {
@@ -438,7 +445,38 @@ __device__ __forceinline__ void process_tile_flat(const StepArgs& a, float* __re
       sh[p] = fadd(d, sb[p]);
     });
   } else {
-    ring_for<0, T::NB - 1>(tid, [&](int p) { sh[p] = fadd(sd[p], sb[p]); });
+    ring_for<0, T::NB - 1, INTERIOR>(tid, [&](int p) { sh[p] = fadd(sd[p], sb[p]); });
+  }
+  // The flux of cell p as the TMA box holds it (float4 records, or halves).
+  auto box_flux = [&](int p) -> float4 {
+    if constexpr (F16) {
+      const __half2* st = reinterpret_cast<const __half2*>(fbox);
+      const float2 lo = fmul2(__half22float2(st[2 * p]), finv2);
+      const float2 hi = fmul2(__half22float2(st[2 * p + 1]), finv2);
+      return make_float4(lo.x, lo.y, hi.x, hi.y);
+    } else {
+      return reinterpret_cast<const float4*>(fbox)[p];
+    }
+  };
+  if constexpr (!INTERIOR) {
+    // Edge tiles turn the box into planes first (all reads, then all writes:
+    // the planes overwrite the box), so that every step reads planes.
+    constexpr int F = first(T::RF), N = last(T::RF) - F + 1;
+    constexpr int IT = (N + kThreads - 1) / kThreads;
+    float4 w[IT];
+#pragma unroll
+    for (int it = 0; it < IT; ++it)
+      if (it * kThreads + tid < N) w[it] = box_flux(F + it * kThreads + tid);
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < IT; ++it)
+      if (it * kThreads + tid < N) {
+        const int p = F + it * kThreads + tid;
+        fx[p] = w[it].x;
+        fy[p] = w[it].y;
+        fz[p] = w[it].z;
+        fw[p] = w[it].w;
+      }
   }
   __syncthreads();
 
@@ -448,17 +486,8 @@ __device__ __forceinline__ void process_tile_flat(const StepArgs& a, float* __re
     constexpr int s = decltype(s_)::value;
     int gx = 0, gy = 0;
     if (!cell(p, gx, gy)) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // stays zero
-    float4 fo;
-    if constexpr (s > 0) {
-      fo = make_float4(fx[p], fy[p], fz[p], fw[p]);
-    } else if constexpr (F16) {
-      const __half2* st = reinterpret_cast<const __half2*>(fbox);
-      const float2 lo = fmul2(__half22float2(st[2 * p]), finv2);
-      const float2 hi = fmul2(__half22float2(st[2 * p + 1]), finv2);
-      fo = make_float4(lo.x, lo.y, hi.x, hi.y);
-    } else {
-      fo = reinterpret_cast<const float4*>(fbox)[p];
-    }
+    const float4 fo =
+        (s > 0 || !INTERIOR) ? make_float4(fx[p], fy[p], fz[p], fw[p]) : box_flux(p);
     const float hc = sh[p];
     const float2 hc2 = make_float2(hc, hc);
     const float2 ex = fsub2(hc2, make_float2(sh[p + 1], sh[p - 1]));  // (+x, -x)
@@ -556,7 +585,7 @@ __device__ __forceinline__ void process_tile_flat(const StepArgs& a, float* __re
   auto step = [&](auto s_) {
     constexpr int s = decltype(s_)::value;
     constexpr int rf = T::RF - 2 * s;
-    if constexpr (s == 0) {
+    if constexpr (s == 0 && INTERIOR) {
       // the planes overwrite the box: all reads first, then all writes
       constexpr int F = first(rf), N = last(rf) - F + 1;
       constexpr int IT = (N + kThreads - 1) / kThreads;
@@ -569,11 +598,11 @@ __device__ __forceinline__ void process_tile_flat(const StepArgs& a, float* __re
       for (int it = 0; it < IT; ++it)
         if (it * kThreads + tid < N) store(F + it * kThreads + tid, r[it]);
     } else {
-      ring_for<first(rf), last(rf)>(tid, [&](int p) { store(p, outflow(p, s_)); });
+      ring_for<first(rf), last(rf), INTERIOR>(tid, [&](int p) { store(p, outflow(p, s_)); });
     }
     __syncthreads();
     if constexpr (s < K - 1) {
-      ring_for<first(rf - 1), last(rf - 1)>(tid, depth);
+      ring_for<first(rf - 1), last(rf - 1), INTERIOR>(tid, depth);
       __syncthreads();
     } else {
       finish();
@@ -697,30 +726,24 @@ __device__ __forceinline__ void tensormap_acquire(const void* tm) {
 }
 
 // Many grids of different sizes advance in one launch.  Work units are the
-// tiles of every member grid, numbered grid by grid (unit_base); CTA u takes
-// unit u, finds its grid by binary search, loads the tile through that
-// grid's tensor maps and runs the same per-tile steps as step_kernel.  One
-// CTA per unit (the launch has at least as many CTAs as units; the rest
-// return at once): a persistent loop over units would keep its state live
+// tiles of every member grid; CTA u takes units[u], which names its grid and
+// tile, so one load stands between the CTA's start and its tile load (the
+// single-grid kernel has none).  One CTA per unit (the rest of the launch
+// returns at once): a persistent loop over units would keep its state live
 // across the tile and push the tile code into register spills.  Launch
 // `launch_idx` of a chain skips grids that have taken all their launches, so
-// grids with different step counts share a chain.
+// grids with different step counts share a chain.  The CTA then runs the
+// same per-tile steps as step_kernel.
 template <int K, int TX, int TY, bool F16, bool UNI, int MINB>
 __global__ void __launch_bounds__(kThreads, MINB)
-    batch_kernel(const BatchGrid* __restrict__ grids, const int* __restrict__ unit_base,
-                 const int* __restrict__ hdr, int launch_idx) {
+    batch_kernel(const BatchGrid* __restrict__ grids, const BatchUnit* __restrict__ units,
+                 int launch_idx) {
   using T = Tile<K, TX, TY, F16, 1, UNI>;
-  const int ngrids = hdr[0];
-  const int u = blockIdx.x;
-  if (u >= __ldg(unit_base + ngrids)) return;
-  int lo = 0, hi = ngrids - 1;  // last grid whose first unit is <= u
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (__ldg(unit_base + mid) <= u) lo = mid;
-    else hi = mid - 1;
-  }
-  const BatchGrid& G = grids[lo];
-  if (launch_idx >= G.launches) return;
+  const int4 un = __ldg(reinterpret_cast<const int4*>(units) + blockIdx.x);
+  if (launch_idx >= (un.w & 0x3fffffff)) return;
+  const BatchGrid& G = grids[un.x];
+  const int x0 = un.y, y0 = un.z;
+  const int p = ((un.w >> 30) + launch_idx) & 1;
 
   extern __shared__ __align__(128) unsigned char smem_raw[];
   unsigned char* smem = align_smem(smem_raw);
@@ -731,11 +754,7 @@ __global__ void __launch_bounds__(kThreads, MINB)
   float4* sf = (F16 && !UNI) ? reinterpret_cast<float4*>(smem + T::OFF_WORK)
                              : reinterpret_cast<float4*>(smem + T::ST_F);
   const int tid = threadIdx.x;
-  const int t = u - __ldg(unit_base + lo);
-  const int x0 = (t % G.tiles_x) * TX, y0 = (t / G.tiles_x) * TY;
-  const int p = (G.cur + launch_idx) & 1;
   const StepArgs& a = G.a;
-
   if (tid == 0) {
     mbar_init(bar, 1);
     fence_mbar_init();
@@ -1011,7 +1030,7 @@ cudaError_t launch_step(int variant, int flux_storage, const CUtensorMap* tm_b,
 // ---- batched variants ---------------------------------------------------------
 namespace {
 
-using BatchFn = void (*)(const BatchGrid*, const int*, const int*, int);
+using BatchFn = void (*)(const BatchGrid*, const BatchUnit*, int);
 
 struct BatchEntry {
   int k, tx, ty, uni;
@@ -1098,7 +1117,7 @@ cudaError_t prepare_batch_variant(int variant, int flux_storage) {
 }
 
 cudaError_t launch_batch_step(int variant, int flux_storage, const BatchGrid* grids,
-                              const int* unit_base, const int* hdr, int launch_idx, int blocks,
+                              const BatchUnit* units, int launch_idx, int blocks,
                               cudaStream_t s) {
   cudaError_t err = prepare_batch_variant(variant, flux_storage);
   if (err != cudaSuccess) return err;
@@ -1106,7 +1125,7 @@ cudaError_t launch_batch_step(int variant, int flux_storage, const BatchGrid* gr
   const int fs = flux_storage == TWS_FLUX_F16 ? TWS_FLUX_F16 : TWS_FLUX_F32;
   BatchEntry& e = batch_table().e[variant];
   auto fn = reinterpret_cast<BatchFn>(const_cast<void*>(e.fn[fs]));
-  fn<<<blocks, kThreads, e.smem[fs], s>>>(grids, unit_base, hdr, launch_idx);
+  fn<<<blocks, kThreads, e.smem[fs], s>>>(grids, units, launch_idx);
   count_launch();
   return cudaGetLastError();
 }

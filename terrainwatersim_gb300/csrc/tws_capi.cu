@@ -28,6 +28,8 @@ using namespace tws;
 struct VariantMaps {
   bool ready = false;
   CUtensorMap b, d[2], f[2];
+  bool on_device = false;  // copied to the grid's descriptor block (batched kernel)
+  bool fresh = false;      // copied since the last chain that used it
 };
 
 struct tws_grid {
@@ -54,6 +56,7 @@ struct tws_grid {
   double vol_host[1] = {0.0};
   int* err = nullptr;     // device error word
   int err_host[1] = {0};
+  CUtensorMap* desc = nullptr;  // device copies of the maps, 5 per variant (batched kernel)
   long long wait_cycles = kDefaultWaitCycles;  // SM clocks a tile-load wait may take
   int missing_tx = 0;     // test hook: bytes each tile load declares but never moves
   tws_batch* batch = nullptr;  // batch this grid belongs to (its stream is the batch's)
@@ -327,7 +330,7 @@ TWS_API int tws_create(int width, int height, const tws_sim_params* params, int 
   const size_t ob = take(n * 4), od0 = take(n * 4), od1 = take(n * 4), of0 = take(n * fb),
                of1 = take(n * fb), ov = take(n * 8),
                op = take(sizeof(double) * volume_partials_needed()), oo = take(sizeof(double)),
-               oe = take(sizeof(int));
+               oe = take(sizeof(int)), ot = take(sizeof(CUtensorMap) * 5 * step_variant_count());
   cudaMemPool_t pool = library_pool(g->device);
   if (!pool || cudaMallocFromPoolAsync(reinterpret_cast<void**>(&g->slab), off, pool, g->stream) !=
                    cudaSuccess) {
@@ -343,6 +346,7 @@ TWS_API int tws_create(int width, int height, const tws_sim_params* params, int 
   g->vol_partials = reinterpret_cast<double*>(g->slab + op);
   g->vol_out = reinterpret_cast<double*>(g->slab + oo);
   g->err = reinterpret_cast<int*>(g->slab + oe);
+  g->desc = reinterpret_cast<CUtensorMap*>(g->slab + ot);
   // Zero everything, padding included (the F16 flux map reads the padding
   // cell of odd-width rows and relies on it staying zero).
   cudaMemsetAsync(g->b, 0, n * 4, g->stream);
@@ -885,11 +889,18 @@ int run_chain(tws_batch* b, int variant, const std::vector<int>& launches) {
     if (!maps) return bfail(b, TWS_ERR_CUDA, why);
     BatchGrid& e = hg[m];
     std::memset(&e, 0, sizeof(e));  // padding too, so equal tables compare equal
-    e.tm_b = maps->b;
-    e.tm_d[0] = maps->d[0];
-    e.tm_d[1] = maps->d[1];
-    e.tm_f[0] = maps->f[0];
-    e.tm_f[1] = maps->f[1];
+    if (!maps->on_device) {
+      // written once per (grid, variant); the first chain's CTAs fence them
+      CUtensorMap five[5] = {maps->b, maps->d[0], maps->d[1], maps->f[0], maps->f[1]};
+      if (cudaMemcpyAsync(g->desc + 5 * sv, five, sizeof(five), cudaMemcpyHostToDevice,
+                          b->stream) != cudaSuccess)
+        return bfail(b, TWS_ERR_CUDA, "tensor map copy");
+      maps->on_device = true;
+      maps->fresh = true;
+    }
+    e.tm = g->desc + 5 * sv;
+    e.fence = maps->fresh ? 1 : 0;
+    maps->fresh = false;
     e.a = make_step_args(g);
     e.a.err = b->d_err;
     e.d[0] = g->d[0];

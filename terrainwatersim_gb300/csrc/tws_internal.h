@@ -56,12 +56,16 @@ struct StepVariant {
 enum : int { kKindTile = 0, kKindStream = 1 };
 
 // One member grid of a batch as the batched kernel reads it from device
-// memory: its tensor maps (for both ping-pong buffers), its step arguments and
-// its buffers.  64-byte aligned so the tensor maps inside are aligned.
-struct alignas(64) BatchGrid {
-  CUtensorMap tm_b;
-  CUtensorMap tm_d[2];
-  CUtensorMap tm_f[2];
+// memory: its tensor maps, its step arguments and its buffers.  The maps are
+// not in this table (which the host rewrites between chains) but in a block
+// of the grid's own memory written once per kernel variant: tm[0] terrain,
+// tm[1 + i] depth buffer i, tm[3 + i] flux buffer i.  A CTA makes the
+// tensor-map proxy re-read them (an acquire fence, which costs a descriptor
+// fetch per tile) only in the first chain after they were written: `fence`.
+struct alignas(16) BatchGrid {
+  const CUtensorMap* tm;
+  int fence;
+  int pad0_;
   StepArgs a;     // W, H, pitch, constants, sources, flux scale, error word
   float* d[2];
   void* f[2];

@@ -8,11 +8,14 @@
 //   depth update, flow map   flowApply.comp:32-52
 // The two reference dispatches (Terrain.cpp:253-265) become one kernel: a CTA
 // owns a TX x TY tile of output cells, loads b and d with a 2K-cell halo and
-// the flux with a (2K-1)-cell halo into shared memory with TMA
-// (cp.async.bulk.tensor, completion on an mbarrier), recomputes the halo
-// fluxes it needs, and writes d, f and the flow map of its tile once.
-// Halo cells are recomputed redundantly by neighbouring CTAs, so there is no
-// inter-CTA dependency inside a launch.
+// the flux box into shared memory with TMA (cp.async.bulk.tensor, completion
+// on an mbarrier), recomputes the halo fluxes it needs, and writes d, f and
+// the flow map of its tile once.  Halo cells are recomputed redundantly by
+// neighbouring CTAs, so there is no inter-CTA dependency inside a launch.
+// Two layouts: the separate one (flux box = the (2K-1)-cell halo, 2-D loops,
+// process_tile) and the unified one (flux box = the b/d box, flat loops over
+// one index, flux in channel planes, packed f32x2 arithmetic:
+// process_tile_flat), which the default variants use.
 //
 // STAGES = 2 makes the CTAs persistent: each walks the tiles
 // blockIdx.x, blockIdx.x + gridDim.x, ... and keeps the TMA load of its next
@@ -143,9 +146,9 @@ struct Tile {
   static constexpr int FOFF = (FOY - RF) * FW + (FOX - RF);
   // One stage = what TMA writes for one tile: b, d and the flux box (float4
   // records for F32 storage, the raw halves for F16 storage).  In the unified
-  // layout the flux region always has room for NF float records: the F16
-  // halves are widened to floats in place, and interior tiles keep the flux
-  // there as four channel planes of NB floats (process_tile_flat).
+  // layout the flux region always has room for NF float records: the tile
+  // code keeps the flux there as four channel planes of NB floats
+  // (process_tile_flat).
   static constexpr size_t ST_B = 0;
   static constexpr size_t ST_D = align_up((size_t)NB * 4, 128);
   static constexpr size_t ST_F = align_up(ST_D + (size_t)NB * 4, 128);
@@ -194,15 +197,16 @@ __device__ __forceinline__ void issue_tile(unsigned char* st, uint64_t* bar,
   }
 }
 
-// K steps of one tile whose loads have landed in (sb, sd, sf-or-staging).
-// INTERIOR: the tile's whole b/d box lies inside the grid, so no cell it
-// computes is off the grid or on the border (no bounds or wall checks).
-template <int K, int TX, int TY, bool F16, int STAGES, bool UNI, bool INTERIOR>
+// K steps of one tile of the separate layout whose loads have landed in (sb,
+// sd, sf-or-staging).  INTERIOR: the tile's whole b/d box lies inside the
+// grid, so no cell it computes is off the grid or on the border (no bounds or
+// wall checks).
+template <int K, int TX, int TY, bool F16, int STAGES, bool INTERIOR>
 __device__ __forceinline__ void process_tile(const StepArgs& a, float* __restrict__ d_out,
                                              void* __restrict__ f_out, float2* __restrict__ v_out,
                                              int x0, int y0, uint32_t mask, float* sb, float* sd,
                                              float* sh, float4* sf, const unsigned char* staging) {
-  using T = Tile<K, TX, TY, F16, STAGES, UNI>;
+  using T = Tile<K, TX, TY, F16, STAGES, false>;
   const int tid = threadIdx.x;
   // The per-grid scalars, read once (in the batched kernel `a` lives in
   // global memory; in registers the loops below do not reload them).
@@ -226,27 +230,7 @@ __device__ __forceinline__ void process_tile(const StepArgs& a, float* __restric
   } else {
     for (int idx = tid; idx < T::NB; idx += kThreads) sh[idx] = fadd(sd[idx], sb[idx]);
   }
-  if (F16 && UNI) {
-    // The halves of cell p (bytes 8p..8p+7) widen to the float4 at p (bytes
-    // 16p..16p+15) in place.  Going down in rounds of kThreads cells, round c
-    // writes bytes from 16 kThreads c up, which only hold halves of rounds 2c
-    // and up (already read, behind the barrier); round 0 reads all its
-    // halves before any of its writes.
-    constexpr int IT = (T::NF + kThreads - 1) / kThreads;
-    const __half2* st = reinterpret_cast<const __half2*>(staging);
-#pragma unroll
-    for (int it = IT - 1; it >= 0; --it) {
-      const int idx = it * kThreads + tid;
-      float4 w = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-      if (idx < T::NF) {
-        const float2 lo = __half22float2(st[2 * idx]), hi = __half22float2(st[2 * idx + 1]);
-        w = make_float4(fmul(lo.x, finv), fmul(lo.y, finv), fmul(hi.x, finv), fmul(hi.y, finv));
-      }
-      if (it == 0) __syncthreads();
-      if (idx < T::NF) sf[idx] = w;
-      __syncthreads();
-    }
-  } else if (F16) {
+  if (F16) {
     const __half2* st = reinterpret_cast<const __half2*>(staging);
     for (int idx = tid; idx < T::NF; idx += kThreads) {
       const int i = idx / T::FW, j = idx - (idx / T::FW) * T::FW;
@@ -696,10 +680,10 @@ __global__ void __launch_bounds__(kThreads)
         process_tile_flat<K, TX, TY, F16, STAGES, false>(a, a.d_out, a.f_out, a.v_out, x0, y0,
                                                          mask, sb, sd, sh, st + T::ST_F);
     } else if (interior) {
-      process_tile<K, TX, TY, F16, STAGES, UNI, true>(a, a.d_out, a.f_out, a.v_out, x0, y0, mask,
+      process_tile<K, TX, TY, F16, STAGES, true>(a, a.d_out, a.f_out, a.v_out, x0, y0, mask,
                                                       sb, sd, sh, sf, st + T::ST_F);
     } else {
-      process_tile<K, TX, TY, F16, STAGES, UNI, false>(a, a.d_out, a.f_out, a.v_out, x0, y0, mask,
+      process_tile<K, TX, TY, F16, STAGES, false>(a, a.d_out, a.f_out, a.v_out, x0, y0, mask,
                                                        sb, sd, sh, sf, st + T::ST_F);
     }
     __syncthreads();  // stage s, h and the F16 working copy are free again
@@ -791,10 +775,10 @@ __global__ void __launch_bounds__(kThreads, MINB)
       process_tile_flat<K, TX, TY, F16, 1, false>(a, G.d[p ^ 1], G.f[p ^ 1], G.v, x0, y0, mask,
                                                   sb, sd, sh, smem + T::ST_F);
   } else if (interior) {
-    process_tile<K, TX, TY, F16, 1, UNI, true>(a, G.d[p ^ 1], G.f[p ^ 1], G.v, x0, y0, mask, sb,
+    process_tile<K, TX, TY, F16, 1, true>(a, G.d[p ^ 1], G.f[p ^ 1], G.v, x0, y0, mask, sb,
                                                sd, sh, sf, smem + T::ST_F);
   } else {
-    process_tile<K, TX, TY, F16, 1, UNI, false>(a, G.d[p ^ 1], G.f[p ^ 1], G.v, x0, y0, mask, sb,
+    process_tile<K, TX, TY, F16, 1, false>(a, G.d[p ^ 1], G.f[p ^ 1], G.v, x0, y0, mask, sb,
                                                 sd, sh, sf, smem + T::ST_F);
   }
 }

@@ -1,5 +1,5 @@
-"""GPU tests of batches: many uneven grids advanced by one persistent launch
-per step (chains replayed from CUDA graphs) give, grid by grid, the same bits
+"""GPU tests of batches: many uneven grids advanced by one launch per step
+(chains replayed from CUDA graphs) give, grid by grid, the same bits
 as the oracle -- alone or in the mix, with grids joining and leaving between
 calls, with per-grid step counts, with graphs on or off."""
 from __future__ import annotations
@@ -143,6 +143,40 @@ def test_batch_rejects_mixed_storage_and_double_membership(tws, oracle):
             b1.step_each([1, 2])
     g32.close()
     g16.close()
+
+
+@pytest.mark.parametrize("variant", [1, 4])
+def test_batch_reused_memory_new_tensor_maps(tws, oracle, variant):
+    """A grid is destroyed and new grids take its memory from the pool with
+    different contents and shapes: the tensor maps written into the reused
+    memory must be the ones the batched kernel uses (the first chain after a
+    write fences them), so every result matches the oracle bit for bit."""
+    first = [make_grid(tws, oracle, s) for s in SPECS[:3]]
+    with tws.Batch() as batch:
+        batch.set_variant(variant)
+        for g, _ in first:
+            batch.add(g)
+        batch.step(6)
+        batch.sync()
+        for g, _ in first:
+            batch.remove(g)
+            g.close()
+        # similar sizes, different shapes and contents, likely in the freed memory
+        respec = [(80, 96, 1, 0.99, 11, 9, 0.03), (33, 257, 0, 0.995, 12, 6, 0.02),
+                  (190, 33, 1, 0.998, 13, 5, 0.04)]
+        second = [make_grid(tws, oracle, s) for s in respec]
+        for g, _ in second:
+            batch.add(g)
+        batch.step(10)
+        batch.sync()
+        for g, setup in second:
+            od, of, ov = oracle_state(oracle, setup, 10)
+            gd, gf, gv = g.download()
+            assert_bitexact(gd, od, f"depth {g.width}x{g.height}")
+            assert_bitexact(gf, of, f"flux {g.width}x{g.height}")
+            assert_bitexact(gv, ov, f"velocity {g.width}x{g.height}")
+    for g, _ in second:
+        g.close()
 
 
 def test_batch_autotune_preserves_state(tws, oracle):

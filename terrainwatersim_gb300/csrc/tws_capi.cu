@@ -910,7 +910,6 @@ int run_chain(tws_batch* b, int variant, const std::vector<int>& launches) {
     e.v = g->v;
     e.cur = g->cur;
     e.launches = launches[i];
-    e.tiles_x = (g->W + tx - 1) / tx;
     const int meta = launches[i] | (g->cur << 30);
     for (int y0 = 0; y0 < g->H; y0 += ty)
       for (int x0 = 0; x0 < g->W; x0 += tx) hu[u++] = BatchUnit{m, x0, y0, meta};

@@ -70,10 +70,10 @@ struct alignas(16) BatchGrid {
   float* d[2];
   void* f[2];
   float2* v;
+  // The kernel takes both from the unit records; here they make a changed
+  // chain compare unequal with the table the device holds.
   int cur;        // buffer holding the state when the chain starts
   int launches;   // launches of this chain that advance this grid
-  int tiles_x;
-  int pad_;
 };
 
 // One work unit (tile) of a batched launch, as the batched kernel reads it:

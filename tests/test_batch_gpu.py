@@ -179,6 +179,42 @@ def test_batch_reused_memory_new_tensor_maps(tws, oracle, variant):
         g.close()
 
 
+@pytest.mark.parametrize("flux_storage", [0, 1])
+def test_batch_large_grid_matches_single_grid_path(tws, flux_storage):
+    """A 4096x2048 grid (8192 tiles) batched with small ones gives the same
+    bits as the same grids stepped alone by the single-grid kernel."""
+    specs = [(4096, 2048, 11), (300, 200, 12), (64, 1000, 13)]
+    p = tws.params_physical(boundary=tws.BOUNDARY_CLOSED)
+
+    def make():
+        gs = []
+        for W, H, seed in specs:
+            g = tws.Grid(W, H, p, flux_storage)
+            g.generate_scene(seed, 40.0, 15.0)
+            g.set_sources(tws.rain_disks(seed, W, H, 24, 0.01, 1))
+            gs.append(g)
+        return gs
+
+    alone = make()
+    for g in alone:
+        g.step(10)
+    want = [g.download() for g in alone]
+    for g in alone:
+        g.close()
+    batched = make()
+    with tws.Batch(flux_storage) as batch:
+        for g in batched:
+            batch.add(g)
+        batch.step(10)
+        batch.sync()
+        got = [g.download() for g in batched]
+    for g in batched:
+        g.close()
+    for (W, H, _), w, gg in zip(specs, want, got):
+        for name, a, b in zip(("depth", "flux", "velocity"), gg, w):
+            assert_bitexact(a, b, f"{name} {W}x{H}")
+
+
 def test_batch_autotune_preserves_state(tws, oracle):
     made = [make_grid(tws, oracle, s) for s in SPECS]
     with tws.Batch() as batch:

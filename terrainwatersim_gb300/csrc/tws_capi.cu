@@ -511,12 +511,13 @@ TWS_API int tws_autotune(tws_grid* g, int trial_steps, int* chosen) {
   const size_t cells = (size_t)g->pitch * g->H;
   const size_t fb = flux_bytes_per_cell(g->flux_storage);
   const int steps = (trial_steps + 11) / 12 * 12;  // a multiple of every K
-  float* sd = nullptr;
-  void* sf = nullptr;
-  float2* sv = nullptr;
-  TWS_CUDA(g, cudaMallocAsync(&sd, cells * 4, g->stream), "autotune state copy");
-  TWS_CUDA(g, cudaMallocAsync(&sf, cells * fb, g->stream), "autotune state copy");
-  TWS_CUDA(g, cudaMallocAsync(&sv, cells * 8, g->stream), "autotune state copy");
+  // one allocation for the saved state: depth, flux, flow map
+  char* saved = nullptr;
+  TWS_CUDA(g, cudaMallocAsync(reinterpret_cast<void**>(&saved), cells * (4 + fb + 8), g->stream),
+           "autotune state copy");
+  float* sd = reinterpret_cast<float*>(saved);
+  void* sf = saved + cells * 4;
+  float2* sv = reinterpret_cast<float2*>(saved + cells * (4 + fb));
   const int cur0 = g->cur;
   cudaMemcpyAsync(sd, g->d[cur0], cells * 4, cudaMemcpyDeviceToDevice, g->stream);
   cudaMemcpyAsync(sf, g->f[cur0], cells * fb, cudaMemcpyDeviceToDevice, g->stream);
@@ -552,9 +553,7 @@ TWS_API int tws_autotune(tws_grid* g, int trial_steps, int* chosen) {
     }
   }
   restore();
-  cudaFreeAsync(sd, g->stream);
-  cudaFreeAsync(sf, g->stream);
-  cudaFreeAsync(sv, g->stream);
+  cudaFreeAsync(saved, g->stream);
   cudaStreamSynchronize(g->stream);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -926,11 +925,15 @@ int run_chain(tws_batch* b, int variant, const std::vector<int>& launches) {
   if (same) {
     b->slot = prev ^ 1;  // keep the uploaded copy in its slot for the next comparison
   } else {
-    cudaMemcpyAsync(b->d_grids, hg, sizeof(BatchGrid) * m, cudaMemcpyHostToDevice, b->stream);
-    cudaMemcpyAsync(b->d_units, hu, sizeof(BatchUnit) * blocks, cudaMemcpyHostToDevice,
-                    b->stream);
-    if (!b->copied[s]) cudaEventCreateWithFlags(&b->copied[s], cudaEventDisableTiming);
-    cudaEventRecord(b->copied[s], b->stream);
+    b->uploaded_slot = -1;  // until the copies below are queued
+    if (cudaMemcpyAsync(b->d_grids, hg, sizeof(BatchGrid) * m, cudaMemcpyHostToDevice,
+                        b->stream) != cudaSuccess ||
+        cudaMemcpyAsync(b->d_units, hu, sizeof(BatchUnit) * blocks, cudaMemcpyHostToDevice,
+                        b->stream) != cudaSuccess ||
+        (!b->copied[s] &&
+         cudaEventCreateWithFlags(&b->copied[s], cudaEventDisableTiming) != cudaSuccess) ||
+        cudaEventRecord(b->copied[s], b->stream) != cudaSuccess)
+      return bfail(b, TWS_ERR_CUDA, "batch table upload");
     b->uploaded_slot = s;
     b->uploaded_m = m;
     b->uploaded_blocks = blocks;

@@ -328,7 +328,10 @@ def run_ours(args):
                 "variant": best_v,
                 "tile": [vinfo[best_v][1], vinfo[best_v][2]],
                 "flux_storage": args.flux,
-                "l2": f"state {state_bytes / 1e6:.0f} MB > L2 {L2_BYTES / 1e6:.0f} MB, no flush",
+                "l2": (f"state {state_bytes / 1e6:.0f} MB > L2 {L2_BYTES / 1e6:.0f} MB, no flush"
+                       if state_bytes > L2_BYTES else
+                       f"state {state_bytes / 1e6:.0f} MB fits the {L2_BYTES / 1e6:.0f} MB L2 "
+                       "(no flush; the default 4096^2 workload does not fit)"),
                 "parallelism": "replicas (one whole grid per GPU)" if ws > 1 else "single grid",
             },
             "hbm_frac_of_measured": round(achieved / peak, 4),

@@ -136,6 +136,20 @@ TWS_API int tws_upload_device(tws_grid* grid, const float* terrain, const float*
  * generator is not the benchmark's. */
 TWS_API int tws_generate_scene(tws_grid* grid, uint64_t seed, float height_scale, float fill);
 
+/* Reset to the reference's own scene, Terrain::CreateHeightmapFromNoiseAndResetSim
+ * (Terrain.cpp:200-238), generated on the device: terrain from the reference's
+ * value noise (NoiseGenerator.cpp:12-97; octaves 2..10, persistence 0.43,
+ * periodic) scaled to height_scale (the reference's default: 300), depth
+ * max(0, (0.45 - r^4 * 800) * height_scale - b) with r the distance from the
+ * grid centre in grid units, flux and velocity zero.  The noise table is the
+ * one the reference's Random.cpp gives after Init(seed) (the application uses
+ * TWS_REFERENCE_NOISE_SEED, Application.cpp:57) and `generation` earlier
+ * scenes (0: the first, each reset draws a new table).  The reference's grid
+ * is square; a W x H grid uses 1/(W-1) and 1/(H-1) per axis.  W, H >= 2. */
+#define TWS_REFERENCE_NOISE_SEED 231656522u
+TWS_API int tws_generate_reference_scene(tws_grid* grid, uint32_t seed, int generation,
+                                         float height_scale);
+
 /* Rain disks of the synthetic benchmark scene: `count` DISK sources of the
  * given radius and rate, centres drawn from the PCG32 stream
  * (seed, 1000 + k): cx = r + u0 % (W - 2r), cy = r + u1 % (H - 2r) (grid

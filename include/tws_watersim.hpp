@@ -61,9 +61,22 @@ class WaterSim {
   WaterSim(const WaterSim&) = delete;
   WaterSim& operator=(const WaterSim&) = delete;
 
-  /// Terrain::CreateHeightmapFromNoiseAndResetSim (Terrain.cpp:200-238) with
-  /// the benchmark's seeded generator: terrain in [0, heightScale), depth
-  /// max(0, fill - terrain), outflow and flow map zero.
+  /// Terrain::CreateHeightmapFromNoiseAndResetSim (Terrain.cpp:200-238): the
+  /// reference's own noise terrain (height scale 300, Terrain.cpp:25) and
+  /// central pool, outflow and flow map zero.  Each call draws the next noise
+  /// table, as the reference's application-wide generator (seeded once,
+  /// Application.cpp:57) does, so the first call gives the reference's first
+  /// scene.
+  void CreateHeightmapFromNoiseAndResetSim() {
+    check(tws_generate_reference_scene(m_grid, TWS_REFERENCE_NOISE_SEED, m_noiseScenes,
+                                       m_heightScale),
+          m_grid);
+    ++m_noiseScenes;
+    m_timeSinceLastSimulationStep = 0.0;
+  }
+
+  /// The same reset with the benchmark's seeded generator instead: terrain in
+  /// [0, heightScale), depth max(0, fill - terrain), outflow and flow map zero.
   void CreateHeightmapFromNoiseAndResetSim(uint64_t seed, float heightScale, float fill) {
     check(tws_generate_scene(m_grid, seed, heightScale, fill), m_grid);
     m_timeSinceLastSimulationStep = 0.0;
@@ -165,6 +178,8 @@ class WaterSim {
   float m_flowDamping;
   float m_flowAcceleration;
   double m_timeSinceLastSimulationStep;
+  float m_heightScale = 300.0f;  // Terrain.cpp:25
+  int m_noiseScenes = 0;         // noise tables drawn so far
 };
 
 }  // namespace tws

@@ -252,3 +252,51 @@ def ref_steps(b, d, f, kf, ka, c, nsteps, brush=None):
         R.tws_ref_flow_update(_fp(td), _fp(fl), W, H, _fp(p))
         R.tws_ref_flow_apply(_fp(td), _fp(fl), _fp(fm), W, H, _fp(p))
     return td[..., 3].copy(), fl, fm
+
+
+# --------------------------------------------------------------------------- reference noise scene
+
+REFERENCE_NOISE_SEED = 231656522  # Application.cpp:57
+_REF_NOISE_PATH = os.path.join(HERE, "_ref", "libtws_ref_noise.so")
+_ref_noise = None
+
+
+def reference_noise_table(seed: int = REFERENCE_NOISE_SEED, generation: int = 0) -> np.ndarray:
+    """The 4096-entry white-noise table of the reference's NoiseGenerator after
+    Random::Init(seed) and `generation` earlier generators (the restatement)."""
+    L = lib()
+    L.tws_oracle_reference_noise_table.argtypes = [C.c_uint32, C.c_int, C.c_void_p]
+    t = np.empty(4096, np.float32)
+    L.tws_oracle_reference_noise_table(seed, generation, _fp(t))
+    return t
+
+
+def reference_terrain(W: int, H: int, height_scale: float = 300.0,
+                      seed: int = REFERENCE_NOISE_SEED, generation: int = 0):
+    """The reference's own scene (Terrain::CreateHeightmapFromNoiseAndResetSim),
+    b and d float32 (H, W), from the restatement."""
+    L = lib()
+    L.tws_oracle_reference_terrain.argtypes = [C.c_uint32, C.c_int, C.c_int, C.c_int, C.c_float,
+                                               C.c_void_p, C.c_void_p]
+    b = np.empty((H, W), np.float32)
+    d = np.empty((H, W), np.float32)
+    L.tws_oracle_reference_terrain(seed, generation, W, H, height_scale, _fp(b), _fp(d))
+    return b, d
+
+
+def ref_noise_available() -> bool:
+    return os.path.exists(_REF_NOISE_PATH)
+
+
+def ref_noise():
+    """The reference's own Random.cpp and NoiseGenerator.cpp, built by
+    `make -C oracle ref` (square grids, as the reference)."""
+    global _ref_noise
+    with _lock:
+        if _ref_noise is None:
+            R = C.CDLL(_REF_NOISE_PATH)
+            R.tws_ref_noise_table.argtypes = [C.c_uint, C.c_int, C.c_void_p]
+            R.tws_ref_reference_terrain.argtypes = [C.c_uint, C.c_int, C.c_int, C.c_float,
+                                                    C.c_void_p, C.c_void_p]
+            _ref_noise = R
+    return _ref_noise

@@ -504,3 +504,122 @@ void tws_oracle_terrain_mips(int W, int H, const float* b, const float* d, int l
 int tws_oracle_max_threads(void) { return num_threads(0); }
 
 }  // extern "C"
+
+// ---- the reference's own noise terrain -------------------------------------------
+// Terrain::CreateHeightmapFromNoiseAndResetSim (Terrain.cpp:200-222) fills the
+// heightmap from NoiseGenerator::GetValueNoise (NoiseGenerator.cpp:12-40,
+// GetNoise3D 42-97), whose 4096-entry white-noise table comes from the
+// application-wide generator of Random.cpp (seeded once, Application.cpp:57;
+// each NoiseGenerator takes the next 4096 numbers).  Restated here in the
+// reference's operation order, evaluated left to right with no contraction.
+namespace {
+
+// The table generator of Random.cpp:22-57: a Mersenne-Twister-shaped state of
+// 624 words with the reference's own seeding rule.
+struct RefTableRng {
+  uint32_t st[624];
+  int at = 0;
+  static uint32_t twist(uint32_t lo_word, uint32_t hi_word, uint32_t far) {
+    const uint32_t y = (lo_word & 0x80000000u) | (hi_word & 0x7FFFFFFFu);
+    return far ^ (y >> 1) ^ ((y & 1u) ? 0x9908B0DFu : 0u);
+  }
+  explicit RefTableRng(uint32_t seed) {
+    for (uint32_t k = 0; k < 624; ++k) st[k] = (k & 1u) ? seed + k * 527u : (2135u + seed * 74111u) * k;
+    for (int k = 0; k < 624; ++k) st[k] = twist(st[k], st[(k + 1) % 624], st[(k + 397) % 624]);
+  }
+  float next() {
+    const int nx = (at + 1) % 624;
+    st[at] = twist(st[at], st[nx], st[(at + 397) % 624]);
+    uint32_t y = st[at];
+    at = nx;
+    y ^= y >> 11;
+    y ^= (y << 7) & 0x9D2C5680u;
+    y ^= (y << 15) & 0xEFC60000u;
+    y ^= y >> 18;
+    return static_cast<float>(static_cast<double>(y) * 4.656612874e-10 - 1.0);
+  }
+};
+
+inline float ref_smooth(float f) { return ((f * f) * f) * ((f * ((f * 6.0f) - 15.0f)) + 10.0f); }
+
+inline int ref_floor(float a) {
+  const int r = static_cast<int>(a);
+  return r - static_cast<int>((a < 0.0f) && (a - static_cast<float>(r) != 0.0f));
+}
+
+// Trilinear value noise with quintic weights over a 16^3 table, period <= 16.
+float ref_noise3(const float* table, float cx, float cy, float cz, int period) {
+  period = period < 16 ? period : 16;
+  const int mod = period - 1;
+  int x0 = ref_floor(cx), y0 = ref_floor(cy), z0 = ref_floor(cz);
+  const float fx = cx - static_cast<float>(x0), fy = cy - static_cast<float>(y0),
+              fz = cz - static_cast<float>(z0);
+  x0 = (x0 % period + period) & mod;
+  y0 = (y0 % period + period) & mod;
+  z0 = (z0 % period + period) & mod;
+  const int x1 = (x0 + 1) & mod, y1 = (y0 + 1) & mod, z1 = (z0 + 1) & mod;
+  auto at = [&](int x, int y, int z) { return table[x + 16 * (y + 16 * z)]; };
+  const float s000 = at(x0, y0, z0), s100 = at(x1, y0, z0), s010 = at(x0, y1, z0),
+              s110 = at(x1, y1, z0), s001 = at(x0, y0, z1), s101 = at(x1, y0, z1),
+              s011 = at(x0, y1, z1), s111 = at(x1, y1, z1);
+  const float u = ref_smooth(fx), v = ref_smooth(fy), w = ref_smooth(fz);
+  const float uv = u * v, uw = u * w, vw = v * w;
+  const float k0 = s000, k1 = s100 - s000, k2 = s010 - s000, k3 = s001 - s000;
+  const float k4 = (s110 - s010) - k1;
+  const float k5 = ((s000 - s010) - s001) + s011;
+  const float k6 = ((-k1) - s001) + s101;
+  const float k7 = ((((-k4) + s001) - s101) - s011) + s111;
+  return ((((((k0 + k1 * u) + k2 * v) + k3 * w) + k4 * uv) + k5 * vw) + k6 * uw) + (k7 * uv) * w;
+}
+
+// GetValueNoise with the terrain's arguments: octaves 2..10, persistence 0.43,
+// periodic, z = 0.  Result in [-1, 1].
+float ref_terrain_noise(const float* table, float cx, float cy) {
+  const float persistence = 0.43f;
+  float sum = 0.0f, amplitude = 1.0f, frequency = static_cast<float>(1 << 2);
+  for (int octave = 2; octave <= 10; ++octave) {
+    const float n = ref_noise3(table, cx * frequency, cy * frequency, 0.0f * frequency,
+                               static_cast<int>(frequency));
+    sum = sum + amplitude * ((n * 0.5f) + 0.5f);
+    amplitude = amplitude * persistence;
+    frequency = frequency * 2.0f;
+  }
+  return (((sum * 2.0f) * (1.0f - persistence)) / (1.0f - amplitude)) - 1.0f;
+}
+
+}  // namespace
+
+extern "C" {
+
+// The white-noise table after the generator is seeded with `seed` and
+// `generation` earlier tables were drawn.
+void tws_oracle_reference_noise_table(uint32_t seed, int generation, float* out4096) {
+  RefTableRng rng(seed);
+  for (int g = 0; g < generation; ++g)
+    for (int i = 0; i < 4096; ++i) rng.next();
+  for (int i = 0; i < 4096; ++i) out4096[i] = rng.next();
+}
+
+// The reference scene on a W x H grid (the reference's own is square: W = H):
+// b = (noise(x mx, y my) * 0.5 + 0.5) * hs and d = max(0, (0.45 - len2^2 * 800)
+// * hs - b), len2 = (x mx - 0.5)^2 + (y my - 0.5)^2, mx = 1 / (W - 1), my =
+// 1 / (H - 1).  pow(len2, 2) of the float overload is the rounded square.
+void tws_oracle_reference_terrain(uint32_t seed, int generation, int W, int H, float height_scale,
+                                  float* b, float* d) {
+  std::vector<float> table(4096);
+  tws_oracle_reference_noise_table(seed, generation, table.data());
+  const float mx = 1.0f / static_cast<float>(W - 1), my = 1.0f / static_cast<float>(H - 1);
+#pragma omp parallel for schedule(static)
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      const float fxm = mx * static_cast<float>(x), fym = my * static_cast<float>(y);
+      const float bb = ((ref_terrain_noise(table.data(), fxm, fym) * 0.5f) + 0.5f) * height_scale;
+      const float ex = static_cast<float>(x) * mx - 0.5f, ey = static_cast<float>(y) * my - 0.5f;
+      const float len2 = ex * ex + ey * ey;
+      const float dd = ((0.45f - (len2 * len2) * 800.0f) * height_scale) - bb;
+      b[(size_t)y * W + x] = bb;
+      d[(size_t)y * W + x] = (0.0f < dd) ? dd : 0.0f;
+    }
+}
+
+}  // extern "C"

@@ -39,6 +39,7 @@ ERR_INVALID = -1
 ERR_CUDA = -2
 ERR_OOM = -3
 ERR_TIMEOUT = -4
+REFERENCE_NOISE_SEED = 231656522  # the seed the reference application uses
 ERR_UNSUPPORTED = -5
 ERR_BUSY = -6
 ERR_TOO_LARGE = -7
@@ -98,6 +99,7 @@ def _declare(L):
         "tws_upload": ([vp, vp, vp, vp], i),
         "tws_upload_device": ([vp, vp, vp, vp], i),
         "tws_generate_scene": ([vp, u64, f, f], i),
+        "tws_generate_reference_scene": ([vp, C.c_uint32, i, f], i),
         "tws_scene_rain_disks": ([u64, i, i, i, f, i, vp], i),
         "tws_set_params": ([vp, vp], i),
         "tws_set_sources": ([vp, vp, i], i),
@@ -274,6 +276,13 @@ class Grid:
 
     def generate_scene(self, seed: int, height_scale: float = 40.0, fill: float = 15.0):
         _check(lib().tws_generate_scene(self._h, seed, height_scale, fill), self._h)
+
+    def generate_reference_scene(self, seed: int = REFERENCE_NOISE_SEED, generation: int = 0,
+                                 height_scale: float = 300.0):
+        """The reference's own noise terrain and central pool
+        (Terrain::CreateHeightmapFromNoiseAndResetSim)."""
+        _check(lib().tws_generate_reference_scene(self._h, seed, generation, height_scale),
+               self._h)
 
     def set_params(self, params: SimParams):
         _check(lib().tws_set_params(self._h, C.byref(params)), self._h)

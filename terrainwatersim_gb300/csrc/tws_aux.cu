@@ -302,6 +302,134 @@ cudaError_t launch_flux_from_f32(const float* in_packed, int flux_storage, float
   return cudaGetLastError();
 }
 
+// ---- the reference's own noise terrain ---------------------------------------------
+// Terrain::CreateHeightmapFromNoiseAndResetSim (Terrain.cpp:200-222): the
+// heightmap is NoiseGenerator::GetValueNoise (NoiseGenerator.cpp:12-97) over a
+// 4096-entry white-noise table drawn from the application-wide generator of
+// Random.cpp (seeded once at start-up, Application.cpp:57; every generator
+// takes the next 4096 numbers).  The table is made on the host (4096 numbers
+// of a sequential generator), the per-cell noise on the device, in the
+// reference's operation order with no contraction.
+namespace {
+
+// Random.cpp:22-57: a Mersenne-Twister-shaped state of 624 words, seeded
+// with the reference's own rule.
+class RefTableRng {
+ public:
+  explicit RefTableRng(uint32_t seed) {
+    for (uint32_t k = 0; k < 624; ++k)
+      st_[k] = (k & 1u) ? seed + k * 527u : (2135u + seed * 74111u) * k;
+    for (int k = 0; k < 624; ++k) st_[k] = twist(st_[k], st_[(k + 1) % 624], st_[(k + 397) % 624]);
+  }
+  float next() {
+    const int nx = (at_ + 1) % 624;
+    st_[at_] = twist(st_[at_], st_[nx], st_[(at_ + 397) % 624]);
+    uint32_t y = st_[at_];
+    at_ = nx;
+    y ^= y >> 11;
+    y ^= (y << 7) & 0x9D2C5680u;
+    y ^= (y << 15) & 0xEFC60000u;
+    y ^= y >> 18;
+    return static_cast<float>(static_cast<double>(y) * 4.656612874e-10 - 1.0);
+  }
+
+ private:
+  static uint32_t twist(uint32_t lo_word, uint32_t hi_word, uint32_t far) {
+    const uint32_t y = (lo_word & 0x80000000u) | (hi_word & 0x7FFFFFFFu);
+    return far ^ (y >> 1) ^ ((y & 1u) ? 0x9908B0DFu : 0u);
+  }
+  uint32_t st_[624];
+  int at_ = 0;
+};
+
+__device__ __forceinline__ float ref_smooth(float f) {
+  return fmul(fmul(fmul(f, f), f), fadd(fmul(f, fsub(fmul(f, 6.0f), 15.0f)), 10.0f));
+}
+
+// GetNoise3D for z = 0 (the terrain's only plane; the z terms keep their
+// operations, with weight w = smooth(0) = 0).
+__device__ float ref_noise2(const float* __restrict__ tab, float cx, float cy, int period) {
+  period = period < 16 ? period : 16;
+  const int mod = period - 1;
+  int x0 = (int)cx, y0 = (int)cy;  // cx, cy >= 0: the reference's floor
+  const float fx = fsub(cx, (float)x0), fy = fsub(cy, (float)y0);
+  x0 = (x0 % period + period) & mod;
+  y0 = (y0 % period + period) & mod;
+  const int x1 = (x0 + 1) & mod, y1 = (y0 + 1) & mod;
+  const int z1 = 1 & mod;  // z0 = 0
+  const float s000 = __ldg(tab + x0 + 16 * y0), s100 = __ldg(tab + x1 + 16 * y0);
+  const float s010 = __ldg(tab + x0 + 16 * y1), s110 = __ldg(tab + x1 + 16 * y1);
+  const float s001 = __ldg(tab + x0 + 16 * (y0 + 16 * z1));
+  const float s101 = __ldg(tab + x1 + 16 * (y0 + 16 * z1));
+  const float s011 = __ldg(tab + x0 + 16 * (y1 + 16 * z1));
+  const float s111 = __ldg(tab + x1 + 16 * (y1 + 16 * z1));
+  const float u = ref_smooth(fx), v = ref_smooth(fy), w = ref_smooth(0.0f);
+  const float uv = fmul(u, v), uw = fmul(u, w), vw = fmul(v, w);
+  const float k0 = s000, k1 = fsub(s100, s000), k2 = fsub(s010, s000), k3 = fsub(s001, s000);
+  const float k4 = fsub(fsub(s110, s010), k1);
+  const float k5 = fadd(fsub(fsub(s000, s010), s001), s011);
+  const float k6 = fadd(fsub(-k1, s001), s101);
+  const float k7 = fadd(fsub(fsub(fadd(-k4, s001), s101), s011), s111);
+  float r = fadd(k0, fmul(k1, u));
+  r = fadd(r, fmul(k2, v));
+  r = fadd(r, fmul(k3, w));
+  r = fadd(r, fmul(k4, uv));
+  r = fadd(r, fmul(k5, vw));
+  r = fadd(r, fmul(k6, uw));
+  return fadd(r, fmul(fmul(k7, uv), w));
+}
+
+__global__ void reference_scene_kernel(const float* __restrict__ tab, int W, int H, int pitch,
+                                       float mx, float my, float hs, float* __restrict__ b,
+                                       float* __restrict__ d) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= W || y >= H) return;
+  const float cx = fmul(mx, (float)x), cy = fmul(my, (float)y);
+  // GetValueNoise(octaves 2..10, persistence 0.43, periodic)
+  const float persistence = 0.43f;
+  float sum = 0.0f, amplitude = 1.0f, frequency = 4.0f;
+  for (int octave = 2; octave <= 10; ++octave) {
+    const float n = ref_noise2(tab, fmul(cx, frequency), fmul(cy, frequency), (int)frequency);
+    sum = fadd(sum, fmul(amplitude, fadd(fmul(n, 0.5f), 0.5f)));
+    amplitude = fmul(amplitude, persistence);
+    frequency = fmul(frequency, 2.0f);
+  }
+  const float noise =
+      fsub(fdiv(fmul(fmul(sum, 2.0f), fsub(1.0f, persistence)), fsub(1.0f, amplitude)), 1.0f);
+  const float bb = fmul(fadd(fmul(noise, 0.5f), 0.5f), hs);
+  const float ex = fsub(fmul((float)x, mx), 0.5f), ey = fsub(fmul((float)y, my), 0.5f);
+  const float len2 = fadd(fmul(ex, ex), fmul(ey, ey));
+  const float dd = fsub(fmul(fsub(0.45f, fmul(fmul(len2, len2), 800.0f)), hs), bb);
+  const size_t g = (size_t)y * pitch + x;
+  b[g] = bb;
+  d[g] = max0(dd);
+}
+
+}  // namespace
+
+cudaError_t launch_reference_scene(uint32_t seed, int generation, int W, int H, int pitch,
+                                   float height_scale, float* b, float* d, cudaStream_t st) {
+  if (W < 2 || H < 2 || generation < 0) return cudaErrorInvalidValue;
+  float table[4096];
+  RefTableRng rng(seed);
+  for (long long i = 0; i < 4096LL * generation; ++i) rng.next();
+  for (int i = 0; i < 4096; ++i) table[i] = rng.next();
+  float* dtab = nullptr;
+  cudaError_t e = cudaMallocAsync(&dtab, sizeof(table), st);
+  if (e != cudaSuccess) return e;
+  e = cudaMemcpyAsync(dtab, table, sizeof(table), cudaMemcpyHostToDevice, st);  // staged copy
+  if (e == cudaSuccess) {
+    const float mx = 1.0f / (float)(W - 1), my = 1.0f / (float)(H - 1);
+    dim3 blk(32, 8), grd((W + 31) / 32, (H + 7) / 8);
+    reference_scene_kernel<<<grd, blk, 0, st>>>(dtab, W, H, pitch, mx, my, height_scale, b, d);
+    count_launch();
+    e = cudaGetLastError();
+  }
+  cudaFreeAsync(dtab, st);
+  return e;
+}
+
 }  // namespace tws
 
 extern "C" TWS_API int tws_scene_rain_disks(uint64_t seed, int W, int H, int radius, float rate,

@@ -428,6 +428,23 @@ TWS_API int tws_generate_scene(tws_grid* g, uint64_t seed, float height_scale, f
   return TWS_OK;
 }
 
+TWS_API int tws_generate_reference_scene(tws_grid* g, uint32_t seed, int generation,
+                                         float height_scale) {
+  if (!g || generation < 0 || generation > 4096 || !(height_scale >= 0) ||
+      !std::isfinite(height_scale))
+    return fail(g, TWS_ERR_INVALID, "bad reference scene");
+  if (g->W < 2 || g->H < 2) return fail(g, TWS_ERR_INVALID, "the reference scene needs 2x2 cells");
+  const size_t n = (size_t)g->pitch * g->H;
+  g->cur = 0;
+  TWS_CUDA(g, launch_reference_scene(seed, generation, g->W, g->H, g->pitch, height_scale, g->b,
+                                     g->d[0], g->stream),
+           "reference scene");
+  TWS_CUDA(g, cudaMemsetAsync(g->f[0], 0, n * flux_bytes_per_cell(g->flux_storage), g->stream),
+           "clear flux");
+  TWS_CUDA(g, cudaMemsetAsync(g->v, 0, n * 8, g->stream), "clear velocity");
+  return TWS_OK;
+}
+
 TWS_API int tws_set_params(tws_grid* g, const tws_sim_params* p) {
   if (!g || !params_ok(p)) return fail(g, TWS_ERR_INVALID, "bad parameters");
   g->params = *p;

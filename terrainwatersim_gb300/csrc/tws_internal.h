@@ -125,6 +125,8 @@ cudaError_t launch_volume(const float* d, int W, int H, int pitch, double cell_a
 int volume_partials_needed();
 cudaError_t launch_generate_scene(uint64_t seed, int W, int H, int pitch, float height_scale,
                                   float fill, float* b, float* d, cudaStream_t st);
+cudaError_t launch_reference_scene(uint32_t seed, int generation, int W, int H, int pitch,
+                                   float height_scale, float* b, float* d, cudaStream_t st);
 cudaError_t launch_flux_to_f32(const void* f, int flux_storage, float inv_scale, int W, int H,
                                int pitch, float* out_packed, cudaStream_t st);
 cudaError_t launch_flux_from_f32(const float* in_packed, int flux_storage, float scale, int W,

@@ -4,13 +4,41 @@
 // to compare with the oracle.
 #include <cstdio>
 #include <cstdlib>
+#include <string>
 #include <vector>
 
 #include "tws_watersim.hpp"
 
+// Mode "reference": the reference's own reset, called twice (the second call
+// draws the next noise table, as in the reference application); writes the
+// terrain and depth after the second call.
+static int reference_reset(unsigned N, const char* out) {
+  tws::WaterSim sim(N, (float)N);
+  sim.CreateHeightmapFromNoiseAndResetSim();
+  sim.CreateHeightmapFromNoiseAndResetSim();
+  sim.Sync();
+  std::vector<float> b((size_t)N * N), d((size_t)N * N);
+  if (tws_download_terrain(sim.Handle(), b.data()) != TWS_OK) return 3;
+  sim.Download(d.data(), nullptr, nullptr);
+  FILE* fh = std::fopen(out, "wb");
+  if (!fh) return 2;
+  std::fwrite(b.data(), 4, b.size(), fh);
+  std::fwrite(d.data(), 4, d.size(), fh);
+  std::fclose(fh);
+  return 0;
+}
+
 int main(int argc, char** argv) {
   const unsigned N = argc > 1 ? (unsigned)std::atoi(argv[1]) : 128;
   const char* out = argc > 2 ? argv[2] : "facade_out.bin";
+  if (argc > 3 && std::string(argv[3]) == "reference") {
+    try {
+      return reference_reset(N, out);
+    } catch (const tws::Error& e) {
+      std::fprintf(stderr, "tws error %d: %s\n", e.code(), e.what());
+      return 1;
+    }
+  }
   try {
     tws::WaterSim sim(N, (float)N);
     sim.CreateHeightmapFromNoiseAndResetSim(77, 40.0f, 15.0f);

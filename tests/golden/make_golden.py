@@ -67,6 +67,30 @@ def main():
                             brush=case["brush"], steps=np.int64(case["steps"]), d=d_out, f=f_out,
                             flowmap_f16=fm)
         print(f"wrote {path}: volume {O.volume(d_out):.6f}")
+    write_reference_scene()
+
+
+def write_reference_scene():
+    """The reference's own noise scene (Terrain::CreateHeightmapFromNoiseAndResetSim)
+    from its own Random.cpp / NoiseGenerator.cpp, compiled by `make -C oracle
+    ref`: the application's seed, the first and second scene after start-up,
+    a 96x96 grid at the default height scale 300."""
+    if not O.ref_noise_available():
+        raise SystemExit("reference noise library not built")
+    R = O.ref_noise()
+    out = {}
+    for gen in (0, 1):
+        t = np.empty(4096, np.float32)
+        R.tws_ref_noise_table(O.REFERENCE_NOISE_SEED, gen, O._fp(t))
+        N = 96
+        b = np.empty((N, N), np.float32)
+        d = np.empty((N, N), np.float32)
+        R.tws_ref_reference_terrain(O.REFERENCE_NOISE_SEED, gen, N, 300.0, O._fp(b), O._fp(d))
+        out[f"table{gen}"], out[f"b{gen}"], out[f"d{gen}"] = t, b, d
+    path = os.path.join(HERE, "ref_noise_scene_96.npz")
+    np.savez_compressed(path, seed=np.uint32(O.REFERENCE_NOISE_SEED), height_scale=np.float32(300.0),
+                        **out)
+    print(f"wrote {path}")
 
 
 if __name__ == "__main__":

@@ -66,3 +66,18 @@ def test_cpp_facade_matches_oracle(tmp_path, oracle):
     assert_bitexact(d, od, "depth")
     assert_bitexact(f, of, "flux")
     assert_bitexact(v, ov, "velocity")
+
+
+def test_cpp_facade_reference_reset_matches_oracle(tmp_path, oracle):
+    """WaterSim::CreateHeightmapFromNoiseAndResetSim() called twice gives the
+    reference's second scene after start-up (a new noise table per call)."""
+    N = 160
+    exe = _build(tmp_path)
+    out = str(tmp_path / "scene.bin")
+    r = subprocess.run([exe, str(N), out, "reference"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    body = np.fromfile(out, dtype=np.float32)
+    b, d = body[:N * N].reshape(N, N), body[N * N:].reshape(N, N)
+    ob, od = oracle.reference_terrain(N, N, 300.0, generation=1)
+    assert_bitexact(b, ob, "terrain")
+    assert_bitexact(d, od, "depth")

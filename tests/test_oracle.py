@@ -222,3 +222,32 @@ def test_reference_parameter_derivation(oracle):
         abs(kf - 0.98 ** step) < 1e-7
     assert ka == np.float32(step * 10.0 * 1.0)
     assert c == np.float32(step / 1.0)
+
+
+# ------------------------------------------------------------ the reference's noise scene
+
+def test_reference_noise_scene_matches_fixture(oracle):
+    """The restated noise table and scene equal the reference's own
+    Random.cpp / NoiseGenerator.cpp output (tests/golden/ref_noise_scene_96.npz)."""
+    g = load_golden("ref_noise_scene_96")
+    for gen in (0, 1):
+        t = oracle.reference_noise_table(int(g["seed"]), gen)
+        assert np.array_equal(t.view(np.uint32), g[f"table{gen}"].view(np.uint32))
+        b, d = oracle.reference_terrain(96, 96, float(g["height_scale"]), int(g["seed"]), gen)
+        assert_bitexact(b, g[f"b{gen}"], f"terrain {gen}")
+        assert_bitexact(d, g[f"d{gen}"], f"depth {gen}")
+    assert (g["d0"] > 0).any() and (g["d0"] == 0).any()  # the central pool and dry land
+
+
+@pytest.mark.parametrize("N,gen,seed", [(64, 0, 231656522), (257, 2, 231656522), (130, 1, 7)])
+def test_reference_noise_scene_live(oracle, N, gen, seed):
+    """Against the reference's noise code compiled here (make -C oracle ref)."""
+    if not oracle.ref_noise_available():
+        pytest.skip("reference checkout not available")
+    R = oracle.ref_noise()
+    rb = np.empty((N, N), np.float32)
+    rd = np.empty((N, N), np.float32)
+    R.tws_ref_reference_terrain(seed, gen, N, 300.0, oracle._fp(rb), oracle._fp(rd))
+    b, d = oracle.reference_terrain(N, N, 300.0, seed, gen)
+    assert_bitexact(b, rb, "terrain")
+    assert_bitexact(d, rd, "depth")

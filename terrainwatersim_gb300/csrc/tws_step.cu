@@ -822,7 +822,7 @@ VariantEntry make_entry() {
 
 struct VariantTable {
   static constexpr int kMax = 24;
-  VariantEntry e[kMax];
+  VariantEntry e[kMax + 1];  // one spare slot: an entry past kMax is dropped, not written over n
   int n = 0;
   std::mutex mu;
   VariantTable() {
@@ -857,7 +857,8 @@ struct VariantTable {
   }
   template <int K, int TX, int TY, int STAGES, bool UNI = false>
   void add() {
-    e[n++] = make_entry<K, TX, TY, STAGES, UNI>();
+    e[n] = make_entry<K, TX, TY, STAGES, UNI>();
+    if (n < kMax) ++n;
   }
   void add_stream(int ry) {
     VariantEntry s{};
@@ -868,7 +869,8 @@ struct VariantTable {
     s.v.kind = kKindStream;
     s.v.ry = ry;
     s.v.smem = 0;
-    e[n++] = s;
+    e[n] = s;
+    if (n < kMax) ++n;
   }
 };
 

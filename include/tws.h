@@ -280,6 +280,27 @@ TWS_API int tws_download(tws_grid* grid, float* depth, float* flux, float* veloc
 /* Copy terrain to a host array.  Synchronous. */
 TWS_API int tws_download_terrain(tws_grid* grid, float* terrain);
 
+/* ---- asynchronous host I/O ---------------------------------------------
+ * The same transfers without blocking the host, staged through device
+ * buffers (52 bytes per cell, allocated on first use) and run on two copy
+ * streams of the grid, so that the copies of one state overlap the steps of
+ * another: upload i+1 and download i-1 run while the steps of i do.
+ *
+ * tws_upload_async: the state is replaced by the arrays (same arguments and
+ * meaning as tws_upload) before any step queued after this call runs.
+ * tws_download_async: the state as it stands after every step queued before
+ * this call is copied to the arrays (same arguments as tws_download).
+ * Both return at once.  The arrays must stay valid and the input arrays
+ * unchanged until tws_io_wait (or tws_sync) returns, which also guarantees
+ * that the output arrays hold their results.  Page-locked host arrays make
+ * the copies asynchronous; with pageable ones a call may block until its
+ * copy has run.  A later call of the same direction waits on the device for
+ * the staging buffer of the previous one, never on the host. */
+TWS_API int tws_upload_async(tws_grid* grid, const float* terrain, const float* depth,
+                             const float* flux);
+TWS_API int tws_download_async(tws_grid* grid, float* depth, float* flux, float* velocity);
+TWS_API int tws_io_wait(tws_grid* grid);
+
 /* Device pointers (replaces binding the textures for drawing,
  * Terrain.cpp:288, 323-330). */
 TWS_API int tws_get_buffers(tws_grid* grid, tws_buffers* out);
@@ -382,8 +403,9 @@ TWS_API int tws_server_stats(tws_server* server, double* cell_steps, double* sec
 /* Device bytes a grid of this size holds (tws_create's allocations). */
 TWS_API double tws_grid_bytes(int width, int height, int flux_storage);
 
-/* Block the host until the grid's queued work is done; reports a device-side
- * error (TWS_ERR_TIMEOUT) raised by any kernel of this grid. */
+/* Block the host until the grid's queued work (asynchronous host copies
+ * included) is done; reports a device-side error (TWS_ERR_TIMEOUT) raised by
+ * any kernel of this grid. */
 TWS_API int tws_sync(tws_grid* grid);
 
 /* The grid's CUDA stream (cudaStream_t). */

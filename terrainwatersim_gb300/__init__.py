@@ -116,6 +116,9 @@ def _declare(L):
         "tws_volume_noalloc": ([vp, i, i, i, d, vp, vp], i),
         "tws_download": ([vp, vp, vp, vp], i),
         "tws_download_terrain": ([vp, vp], i),
+        "tws_upload_async": ([vp, vp, vp, vp], i),
+        "tws_download_async": ([vp, vp, vp, vp], i),
+        "tws_io_wait": ([vp], i),
         "tws_get_buffers": ([vp, vp], i),
         "tws_sync": ([vp], i),
         "tws_stream": ([vp], vp),
@@ -221,6 +224,15 @@ def _host_f32(a, shape):
     return a
 
 
+def _check_out_f32(a, shape):
+    """An output array the library writes in place: no conversion allowed."""
+    if not isinstance(a, np.ndarray) or a.dtype != np.float32 or not a.flags.c_contiguous \
+            or not a.flags.writeable:
+        raise ValueError("outputs must be writeable C-contiguous float32 numpy arrays")
+    if a.shape != shape:
+        raise ValueError(f"expected shape {shape}, got {a.shape}")
+
+
 class Grid:
     """One simulated grid resident on the GPU (the simulation half of Terrain)."""
 
@@ -233,12 +245,14 @@ class Grid:
         _check(lib().tws_create(self.width, self.height, C.byref(self.params), flux_storage,
                                 C.c_void_p(stream) if stream else None, C.byref(h)))
         self._h = h
+        self._io_refs = []  # host arrays of asynchronous copies not yet waited for
 
     # -- lifecycle
     def close(self):
         if getattr(self, "_h", None):
-            lib().tws_destroy(self._h)
+            lib().tws_destroy(self._h)  # waits for the asynchronous copies
             self._h = None
+            self._io_refs = []
 
     def __enter__(self):
         return self
@@ -269,6 +283,40 @@ class Grid:
         _check(lib().tws_upload(self._h, b.ctypes.data,
                                 d.ctypes.data if d is not None else None,
                                 f.ctypes.data if f is not None else None), self._h)
+
+    def upload_async(self, terrain, depth=None, flux=None):
+        """tws_upload_async: the state is replaced by these arrays before any
+        step queued later; returns at once.  The arrays are kept referenced
+        until io_wait/sync and must not change before then (pinned arrays,
+        e.g. from torch's pin_memory, make the copy asynchronous)."""
+        H, W = self.height, self.width
+        b = _host_f32(terrain, (H, W))
+        d = _host_f32(depth, (H, W)) if depth is not None else None
+        f = _host_f32(flux, (H, W, 4)) if flux is not None else None
+        _check(lib().tws_upload_async(self._h, b.ctypes.data,
+                                      d.ctypes.data if d is not None else None,
+                                      f.ctypes.data if f is not None else None), self._h)
+        self._io_refs.append((b, d, f))
+
+    def download_async(self, out):
+        """tws_download_async into the preallocated (d, f, v) float32 arrays
+        (any may be None): the state after every step queued so far.  The
+        arrays hold it once io_wait/sync returns."""
+        H, W = self.height, self.width
+        d, f, v = out
+        shapes = ((H, W), (H, W, 4), (H, W, 2))
+        for a, shape in zip(out, shapes):
+            if a is not None:
+                _check_out_f32(a, shape)
+        _check(lib().tws_download_async(self._h, d.ctypes.data if d is not None else None,
+                                        f.ctypes.data if f is not None else None,
+                                        v.ctypes.data if v is not None else None), self._h)
+        self._io_refs.append((d, f, v))
+
+    def io_wait(self):
+        """Block until every asynchronous upload and download has completed."""
+        _check(lib().tws_io_wait(self._h), self._h)
+        self._io_refs = []
 
     def upload_device(self, terrain_ptr: int, depth_ptr: int | None = None,
                       flux_ptr: int | None = None):
@@ -332,6 +380,7 @@ class Grid:
 
     def sync(self):
         _check(lib().tws_sync(self._h), self._h)
+        self._io_refs = []
 
     def download(self, depth=True, flux=True, velocity=True, out=None):
         """Return (d, f, v) as float32 host arrays (None where not requested).

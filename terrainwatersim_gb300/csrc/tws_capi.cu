@@ -61,6 +61,16 @@ struct tws_grid {
   int missing_tx = 0;     // test hook: bytes each tile load declares but never moves
   tws_batch* batch = nullptr;  // batch this grid belongs to (its stream is the batch's)
   cudaStream_t home_stream = nullptr;
+  // Asynchronous host I/O, made on first use: packed staging (upload b, d, f
+  // then download d, f, v; 52 bytes per cell), a copy stream per direction,
+  // and the events that hand each staging buffer between a copy stream and
+  // the grid's stream.
+  char* io_slab = nullptr;
+  cudaStream_t io_up = nullptr, io_down = nullptr;
+  cudaEvent_t up_copied = nullptr;    // host -> staging done
+  cudaEvent_t up_consumed = nullptr;  // staging -> state done
+  cudaEvent_t down_staged = nullptr;  // state -> staging done
+  cudaEvent_t down_copied = nullptr;  // staging -> host done
   std::string last_error;
 };
 
@@ -364,8 +374,16 @@ TWS_API int tws_create(int width, int height, const tws_sim_params* params, int 
 TWS_API int tws_destroy(tws_grid* g) {
   if (!g) return TWS_ERR_INVALID;
   if (g->batch) tws_batch_remove(g->batch, g);
+  // the copy streams may still read or write caller arrays: let them finish
+  if (g->io_up) cudaStreamSynchronize(g->io_up);
+  if (g->io_down) cudaStreamSynchronize(g->io_down);
   // stream-ordered: the memory returns to the pool once the grid's queued
   // work is done, without waiting here
+  if (g->io_slab) cudaFreeAsync(g->io_slab, g->stream);
+  for (cudaEvent_t ev : {g->up_copied, g->up_consumed, g->down_staged, g->down_copied})
+    if (ev) cudaEventDestroy(ev);
+  if (g->io_up) cudaStreamDestroy(g->io_up);
+  if (g->io_down) cudaStreamDestroy(g->io_down);
   if (g->slab) cudaFreeAsync(g->slab, g->stream);
   if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
   delete g;
@@ -642,6 +660,169 @@ TWS_API int tws_download_terrain(tws_grid* g, float* b) {
   return TWS_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Staging of the asynchronous host I/O: W x H packed arrays, each starting
+// on a 256-byte boundary (the flux conversions move float4s), upload side
+// (b, d, f as 4 floats) then download side (d, f as 4 floats, v as 2).
+struct IoStaging {
+  float *up_b, *up_d, *up_f, *down_d, *down_f, *down_v;
+};
+
+// Byte offsets of the six arrays for W x H = m cells; returns the total.
+size_t io_layout(size_t m, size_t off[6]) {
+  const size_t floats[6] = {m, m, 4 * m, m, 4 * m, 2 * m};
+  size_t o = 0;
+  for (int i = 0; i < 6; ++i) {
+    off[i] = o;
+    o += (floats[i] * 4 + 255) / 256 * 256;
+  }
+  return o;
+}
+
+IoStaging io_staging(const tws_grid* g) {
+  size_t off[6];
+  io_layout((size_t)g->W * g->H, off);
+  float* a[6];
+  for (int i = 0; i < 6; ++i) a[i] = reinterpret_cast<float*>(g->io_slab + off[i]);
+  return {a[0], a[1], a[2], a[3], a[4], a[5]};
+}
+
+// All or nothing: the grid has the staging, both copy streams and the four
+// events, or none of them.
+int ensure_io(tws_grid* g) {
+  if (g->io_slab) return TWS_OK;
+  cudaStream_t up = nullptr, down = nullptr;
+  cudaEvent_t ev[4] = {};
+  char* slab = nullptr;
+  bool ok = cudaStreamCreateWithFlags(&up, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaStreamCreateWithFlags(&down, cudaStreamNonBlocking) == cudaSuccess;
+  for (int i = 0; ok && i < 4; ++i)
+    ok = cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming) == cudaSuccess;
+  cudaMemPool_t pool = ok ? library_pool(g->device) : nullptr;
+  size_t off[6];
+  const size_t bytes = io_layout((size_t)g->W * g->H, off);
+  ok = ok && pool &&
+       cudaMallocFromPoolAsync(reinterpret_cast<void**>(&slab), bytes, pool, g->stream) ==
+           cudaSuccess;
+  // the copy streams touch the staging only once its allocation has happened
+  ok = ok && cudaStreamSynchronize(g->stream) == cudaSuccess;
+  if (!ok) {
+    const cudaError_t e = cudaGetLastError();
+    if (slab) cudaFreeAsync(slab, g->stream);
+    for (cudaEvent_t x : ev)
+      if (x) cudaEventDestroy(x);
+    if (up) cudaStreamDestroy(up);
+    if (down) cudaStreamDestroy(down);
+    return cuda_fail(g, e == cudaSuccess ? cudaErrorMemoryAllocation : e, "host I/O staging");
+  }
+  g->io_slab = slab;
+  g->io_up = up;
+  g->io_down = down;
+  g->up_copied = ev[0];
+  g->up_consumed = ev[1];
+  g->down_staged = ev[2];
+  g->down_copied = ev[3];
+  return TWS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+TWS_API int tws_upload_async(tws_grid* g, const float* b, const float* d, const float* f) {
+  if (!g || !b) return fail(g, TWS_ERR_INVALID, "terrain array is required");
+  if (const int rc = ensure_io(g)) return rc;
+  const IoStaging s = io_staging(g);
+  const size_t m = (size_t)g->W * g->H, n = (size_t)g->pitch * g->H;
+  const size_t row = (size_t)g->W * 4, pitch = (size_t)g->pitch * 4;
+  // host -> staging on the upload stream, once the previous upload has left
+  // the staging
+  TWS_CUDA(g, cudaStreamWaitEvent(g->io_up, g->up_consumed, 0), "upload order");
+  TWS_CUDA(g, cudaMemcpyAsync(s.up_b, b, m * 4, cudaMemcpyHostToDevice, g->io_up), "upload terrain");
+  if (d)
+    TWS_CUDA(g, cudaMemcpyAsync(s.up_d, d, m * 4, cudaMemcpyHostToDevice, g->io_up), "upload depth");
+  if (f)
+    TWS_CUDA(g, cudaMemcpyAsync(s.up_f, f, m * 16, cudaMemcpyHostToDevice, g->io_up), "upload flux");
+  TWS_CUDA(g, cudaEventRecord(g->up_copied, g->io_up), "upload order");
+  // staging -> state in the grid's stream order
+  TWS_CUDA(g, cudaStreamWaitEvent(g->stream, g->up_copied, 0), "upload order");
+  g->cur = 0;
+  TWS_CUDA(g, cudaMemcpy2DAsync(g->b, pitch, s.up_b, row, row, g->H, cudaMemcpyDeviceToDevice,
+                                g->stream),
+           "stage terrain");
+  if (d)
+    TWS_CUDA(g, cudaMemcpy2DAsync(g->d[0], pitch, s.up_d, row, row, g->H, cudaMemcpyDeviceToDevice,
+                                  g->stream),
+             "stage depth");
+  else
+    TWS_CUDA(g, cudaMemsetAsync(g->d[0], 0, n * 4, g->stream), "clear depth");
+  if (f && g->flux_storage == TWS_FLUX_F32)
+    TWS_CUDA(g, cudaMemcpy2DAsync(g->f[0], (size_t)g->pitch * 16, s.up_f, (size_t)g->W * 16,
+                                  (size_t)g->W * 16, g->H, cudaMemcpyDeviceToDevice, g->stream),
+             "stage flux");
+  else if (f)
+    TWS_CUDA(g, launch_flux_from_f32(s.up_f, g->flux_storage, g->flux_scale, g->W, g->H, g->pitch,
+                                     g->f[0], g->stream),
+             "stage flux");
+  else
+    TWS_CUDA(g, cudaMemsetAsync(g->f[0], 0, n * flux_bytes_per_cell(g->flux_storage), g->stream),
+             "clear flux");
+  TWS_CUDA(g, cudaMemsetAsync(g->v, 0, n * 8, g->stream), "clear velocity");
+  TWS_CUDA(g, cudaEventRecord(g->up_consumed, g->stream), "upload order");
+  return TWS_OK;
+}
+
+TWS_API int tws_download_async(tws_grid* g, float* d, float* f, float* v) {
+  if (!g) return TWS_ERR_INVALID;
+  if (const int rc = ensure_io(g)) return rc;
+  const IoStaging s = io_staging(g);
+  const size_t m = (size_t)g->W * g->H;
+  const size_t row = (size_t)g->W * 4, pitch = (size_t)g->pitch * 4;
+  // state -> staging in the grid's stream order, once the previous download
+  // has left the staging
+  TWS_CUDA(g, cudaStreamWaitEvent(g->stream, g->down_copied, 0), "download order");
+  if (d)
+    TWS_CUDA(g, cudaMemcpy2DAsync(s.down_d, row, g->d[g->cur], pitch, row, g->H,
+                                  cudaMemcpyDeviceToDevice, g->stream),
+             "stage depth");
+  if (f && g->flux_storage == TWS_FLUX_F32)
+    TWS_CUDA(g, cudaMemcpy2DAsync(s.down_f, (size_t)g->W * 16, g->f[g->cur], (size_t)g->pitch * 16,
+                                  (size_t)g->W * 16, g->H, cudaMemcpyDeviceToDevice, g->stream),
+             "stage flux");
+  else if (f)
+    TWS_CUDA(g, launch_flux_to_f32(g->f[g->cur], g->flux_storage, 1.0f / g->flux_scale, g->W, g->H,
+                                   g->pitch, s.down_f, g->stream),
+             "stage flux");
+  if (v)
+    TWS_CUDA(g, cudaMemcpy2DAsync(s.down_v, (size_t)g->W * 8, g->v, (size_t)g->pitch * 8,
+                                  (size_t)g->W * 8, g->H, cudaMemcpyDeviceToDevice, g->stream),
+             "stage velocity");
+  TWS_CUDA(g, cudaEventRecord(g->down_staged, g->stream), "download order");
+  // staging -> host on the download stream
+  TWS_CUDA(g, cudaStreamWaitEvent(g->io_down, g->down_staged, 0), "download order");
+  if (d)
+    TWS_CUDA(g, cudaMemcpyAsync(d, s.down_d, m * 4, cudaMemcpyDeviceToHost, g->io_down),
+             "download depth");
+  if (f)
+    TWS_CUDA(g, cudaMemcpyAsync(f, s.down_f, m * 16, cudaMemcpyDeviceToHost, g->io_down),
+             "download flux");
+  if (v)
+    TWS_CUDA(g, cudaMemcpyAsync(v, s.down_v, m * 8, cudaMemcpyDeviceToHost, g->io_down),
+             "download velocity");
+  TWS_CUDA(g, cudaEventRecord(g->down_copied, g->io_down), "download order");
+  return TWS_OK;
+}
+
+TWS_API int tws_io_wait(tws_grid* g) {
+  if (!g) return TWS_ERR_INVALID;
+  if (g->io_up) TWS_CUDA(g, cudaStreamSynchronize(g->io_up), "upload");
+  if (g->io_down) TWS_CUDA(g, cudaStreamSynchronize(g->io_down), "download");
+  return TWS_OK;
+}
+
 TWS_API int tws_surface(tws_grid* g, const tws_surface_out* o) {
   if (!g || !o) return fail(g, TWS_ERR_INVALID, "null surface output");
   TWS_CUDA(g, launch_surface(g->b, g->d[g->cur], g->v, g->W, g->H, g->pitch, *o, g->stream),
@@ -682,6 +863,7 @@ TWS_API int tws_get_buffers(tws_grid* g, tws_buffers* out) {
 
 TWS_API int tws_sync(tws_grid* g) {
   if (!g) return TWS_ERR_INVALID;
+  if (const int rc = tws_io_wait(g)) return rc;
   TWS_CUDA(g, cudaMemcpyAsync(g->err_host, g->err, sizeof(int), cudaMemcpyDeviceToHost, g->stream),
            "error word copy");
   TWS_CUDA(g, cudaStreamSynchronize(g->stream), "sync");

@@ -563,6 +563,35 @@ def run_c1(args):
                [(s[0], s[1], s[2], s[3], 0.01) for s in rain], nsteps=steps)
     v64 = O.volume(d64)
     g.close()
+    resident = None
+    if tws.resident_fits(W, H):
+        # the same 1000 steps with the grid held in one cluster's shared memory
+        g = tws.Grid(W, H, p, stream=stream.cuda_stream)
+        g.set_sources(rain)
+        g.set_resident(True)
+        for _ in range(3):
+            g.generate_scene(2026, 40.0, 15.0)
+            g.step(steps)
+        g.generate_scene(2026, 40.0, 15.0)
+        torch.cuda.synchronize()
+        n0 = tws.lib().tws_launch_count()
+        ev[0].record(stream)
+        g.step(steps)
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+        rt = ev[0].elapsed_time(ev[1]) / 1e3
+        launches = int(tws.lib().tws_launch_count() - n0)
+        rd, rf, rv = g.download()
+        g.close()
+        resident = {
+            "kernel": "resident_kernel (one 16-CTA cluster, state in distributed shared memory)",
+            "gcell_steps_per_s": round(W * H * steps / rt / 1e9, 3),
+            "step_us_mean": round(rt / steps * 1e6, 3),
+            "launches": launches,
+            "bitexact_vs_fp32_oracle": bool(np.array_equal(rd.view(np.uint32), od.view(np.uint32))
+                                            and np.array_equal(rf.view(np.uint32), of.view(np.uint32))
+                                            and np.array_equal(rv.view(np.uint32), ov.view(np.uint32))),
+        }
     return {
         "config": "256x256 FP32, closed walls, rain r=16 +0.01 m/step, 1000 steps, one launch per step",
         "gcell_steps_per_s": round(W * H * steps / total / 1e9, 3),
@@ -575,6 +604,7 @@ def run_c1(args):
         "rel_volume_diff_vs_fp32_oracle": abs(vol - O.volume(od)) / O.volume(od),
         "max_abs_depth_err_vs_fp64": float(np.abs(d - d64).max()),
         "rel_volume_drift_vs_fp64": abs(vol - v64) / v64,
+        "resident": resident,
     }
 
 

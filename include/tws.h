@@ -204,9 +204,30 @@ TWS_API int tws_test_inject_missing_bytes(tws_grid* grid, int bytes);
  * current state (restored afterwards, so the simulation is unchanged), picks
  * the fastest per cell-step, pins it on this grid and records it for every
  * later grid of the same width, height and flux storage in this process.
- * Synchronous.  `chosen` (may be NULL) receives the variant index.  No
- * counterpart in the reference. */
+ * Where the grid fits the resident kernel (below), that is timed too.
+ * Synchronous.  `chosen` (may be NULL) receives the variant index, or
+ * TWS_VARIANT_RESIDENT if the resident kernel was fastest (it is then turned
+ * on for this grid).  No counterpart in the reference. */
+#define TWS_VARIANT_RESIDENT (-2)
 TWS_API int tws_autotune(tws_grid* grid, int trial_steps, int* chosen);
+
+/* Resident kernel, for small grids: the whole state (28 bytes per cell) sits
+ * in the shared memory of one thread-block cluster of up to 16 SMs, and one
+ * launch runs up to 4096 steps of a tws_step call, the CTAs exchanging their
+ * edge rows through distributed shared memory between the phases of each
+ * step.  It fits grids of up to about 8,000 cells per SM (256 x 256 fits).
+ * Results are bit-identical to the tiled kernels.
+ * tws_resident_fits: the cluster size (CTAs) the automatic choice gives a
+ * grid of this size on the current device, or 0 if it does not fit.
+ * tws_set_resident: `ctas` = TWS_RESIDENT_AUTO turns it on with the automatic
+ * cluster size (one CTA for grids of at most 1024 cells, else the largest
+ * power of two up to 16 that leaves every CTA a row), 1, 2, 4, 8 or 16 with
+ * that many CTAs, 0 turns it off;
+ * TWS_ERR_UNSUPPORTED if the grid does not fit that cluster.
+ * tws_set_variant and tws_set_steps_per_launch turn it off. */
+#define TWS_RESIDENT_AUTO (-1)
+TWS_API int tws_resident_fits(int width, int height, int flux_storage);
+TWS_API int tws_set_resident(tws_grid* grid, int ctas);
 
 /* Advance `nsteps` steps: per step, sources, then the outflow update with
  * non-negativity scaling (flowUpdate.comp:12-63), then the depth update and

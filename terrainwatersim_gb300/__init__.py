@@ -44,6 +44,8 @@ ERR_UNSUPPORTED = -5
 ERR_BUSY = -6
 ERR_TOO_LARGE = -7
 VOLUME_NOALLOC_MAX_ROWS = 16384
+VARIANT_RESIDENT = -2  # tws_autotune's answer when the resident kernel is fastest
+RESIDENT_AUTO = -1     # tws_set_resident: the automatic cluster size
 
 _PKG = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_PKG, "_build", "libtws.so")
@@ -111,6 +113,8 @@ def _declare(L):
         "tws_set_wait_limit": ([vp, C.c_longlong], i),
         "tws_test_inject_missing_bytes": ([vp, i], i),
         "tws_autotune": ([vp, i, vp], i),
+        "tws_resident_fits": ([i, i, i], i),
+        "tws_set_resident": ([vp, i], i),
         "tws_step": ([vp, i], i),
         "tws_volume": ([vp, vp], i),
         "tws_volume_noalloc": ([vp, i, i, i, d, vp, vp], i),
@@ -215,6 +219,12 @@ def variants():
                                   C.byref(sm)))
         out.append((k.value, tx.value, ty.value, st.value, sm.value))
     return out
+
+
+def resident_fits(width: int, height: int, flux_storage: int = FLUX_F32) -> int:
+    """The resident kernel's automatic cluster size (CTAs) for a grid of this
+    size on this device, or 0 if the grid does not fit it."""
+    return int(lib().tws_resident_fits(width, height, flux_storage))
 
 
 def _host_f32(a, shape):
@@ -363,9 +373,17 @@ class Grid:
         so its bounded wait runs out (0 turns it off)."""
         _check(lib().tws_test_inject_missing_bytes(self._h, nbytes), self._h)
 
+    def set_resident(self, on: bool = True, ctas: int | None = None):
+        """Run the steps with the resident kernel (the whole grid in one
+        cluster's shared memory), on `ctas` CTAs (1, 2, 4, 8 or 16; None:
+        the automatic size); raises if the grid does not fit it."""
+        mode = 0 if not on else (RESIDENT_AUTO if ctas is None else int(ctas))
+        _check(lib().tws_set_resident(self._h, mode), self._h)
+
     def autotune(self, trial_steps: int = 24) -> int:
-        """Time every kernel variant on this grid's state (restored after)
-        and pin the fastest; returns its index."""
+        """Time every kernel variant (and the resident kernel, where the grid
+        fits it) on this grid's state (restored after) and use the fastest;
+        returns its index, or VARIANT_RESIDENT."""
         out = C.c_int()
         _check(lib().tws_autotune(self._h, trial_steps, C.byref(out)), self._h)
         return out.value

@@ -47,6 +47,7 @@ struct tws_grid {
   int cur = 0;
   int steps_per_launch = 0;  // 0: library's choice
   int variant = -1;          // pinned kernel variant, -1: automatic
+  int resident = 0;          // > 0: the resident kernel runs the steps, on this many CTAs
   std::vector<VariantMaps> maps;
   tws_source src[TWS_MAX_SOURCES];
   int nsrc = 0;
@@ -181,6 +182,21 @@ int chosen_variant(const tws_grid* g) {
   return step_variant_for(k, g->flux_storage);
 }
 
+// CTAs of the resident kernel if it runs this grid's steps, else 0: it runs
+// them if it was turned on for this grid, or if nothing is pinned and the
+// autotuner chose it for this grid shape (with the automatic cluster size).
+int resident_ctas(const tws_grid* g) {
+  if (g->resident > 0) return g->resident;
+  if (g->variant >= 0 || g->steps_per_launch != 0 || tuned_lookup(g) != TWS_VARIANT_RESIDENT)
+    return 0;
+  int ctas = 0;
+  if (resident_supported(g->W, g->H, g->flux_storage, 0, &ctas) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return ctas;
+}
+
 StepArgs make_step_args(const tws_grid* g) {
   StepArgs a{};
   a.W = g->W;
@@ -203,6 +219,20 @@ StepArgs make_step_args(const tws_grid* g) {
 
 int enqueue_steps(tws_grid* g, int nsteps) {
   StepArgs a = make_step_args(g);
+  if (const int ctas = resident_ctas(g)) {
+    for (int left = nsteps; left > 0;) {
+      const int n = std::min(left, kResidentMaxSteps);
+      const int nxt = g->cur ^ 1;
+      a.d_out = g->d[nxt];
+      a.f_out = g->f[nxt];
+      const cudaError_t e = launch_resident(g->flux_storage, ctas, g->b, g->d[g->cur],
+                                            g->f[g->cur], a, n, g->stream);
+      if (e != cudaSuccess) return cuda_fail(g, e, "resident kernel launch");
+      g->cur = nxt;
+      left -= n;
+    }
+    return TWS_OK;
+  }
   const int main_variant = chosen_variant(g);
   const int kmax = step_variant(main_variant).k;
   int left = nsteps;
@@ -504,6 +534,33 @@ TWS_API int tws_set_steps_per_launch(tws_grid* g, int k) {
   if (!g || k < 0 || k > 4) return fail(g, TWS_ERR_INVALID, "steps per launch must be 0..4");
   g->steps_per_launch = k;
   g->variant = -1;
+  g->resident = 0;
+  return TWS_OK;
+}
+
+TWS_API int tws_resident_fits(int width, int height, int flux_storage) {
+  if (flux_storage != TWS_FLUX_F32 && flux_storage != TWS_FLUX_F16) return 0;
+  int ctas = 0;
+  if (resident_supported(width, height, flux_storage, 0, &ctas) == cudaSuccess) return ctas;
+  cudaGetLastError();
+  return 0;
+}
+
+TWS_API int tws_set_resident(tws_grid* g, int ctas) {
+  if (!g) return TWS_ERR_INVALID;
+  if (ctas < TWS_RESIDENT_AUTO || ctas > 16) return fail(g, TWS_ERR_INVALID, "bad cluster size");
+  int chosen = 0;
+  if (ctas != 0) {
+    const cudaError_t e = resident_supported(g->W, g->H, g->flux_storage,
+                                             ctas == TWS_RESIDENT_AUTO ? 0 : ctas, &chosen);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(g, TWS_ERR_UNSUPPORTED,
+                  std::string("the grid does not fit the resident kernel with this cluster: ") +
+                      cudaGetErrorString(e));
+    }
+  }
+  g->resident = chosen;
   return TWS_OK;
 }
 
@@ -524,6 +581,7 @@ TWS_API int tws_set_variant(tws_grid* g, int variant) {
   if (!g || variant < -1 || variant >= step_variant_count())
     return fail(g, TWS_ERR_INVALID, "no such kernel variant");
   g->variant = variant;
+  g->resident = 0;
   return TWS_OK;
 }
 
@@ -566,7 +624,8 @@ TWS_API int tws_autotune(tws_grid* g, int trial_steps, int* chosen) {
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  const int saved_variant = g->variant;
+  const int saved_variant = g->variant, saved_resident = g->resident;
+  g->resident = 0;
   float best_ms = 1e30f;
   int best = -1, rc = TWS_OK;
   for (int v = 0; v < step_variant_count() && rc == TWS_OK; ++v) {
@@ -587,6 +646,27 @@ TWS_API int tws_autotune(tws_grid* g, int trial_steps, int* chosen) {
       best = v;
     }
   }
+  // the resident kernel, where the grid fits it
+  bool resident_best = false;
+  int res_ctas = 0;
+  if (rc == TWS_OK &&
+      resident_supported(g->W, g->H, g->flux_storage, 0, &res_ctas) == cudaSuccess) {
+    g->resident = res_ctas;
+    float rbest = 1e30f;
+    for (int rep = 0; rep < 2 && rc == TWS_OK; ++rep) {
+      restore();
+      cudaEventRecord(e0, g->stream);
+      rc = enqueue_steps(g, steps);
+      cudaEventRecord(e1, g->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess) rc = TWS_ERR_CUDA;
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      rbest = std::min(rbest, ms);
+    }
+    resident_best = rc == TWS_OK && rbest < best_ms;
+    g->resident = 0;
+  }
+  cudaGetLastError();  // a grid that does not fit leaves the query's error behind
   restore();
   cudaFreeAsync(saved, g->stream);
   cudaStreamSynchronize(g->stream);
@@ -594,14 +674,17 @@ TWS_API int tws_autotune(tws_grid* g, int trial_steps, int* chosen) {
   cudaEventDestroy(e1);
   if (rc != TWS_OK) {
     g->variant = saved_variant;
+    g->resident = saved_resident;
     return rc;
   }
   g->variant = best;
+  g->resident = resident_best ? res_ctas : 0;
+  const int choice = resident_best ? TWS_VARIANT_RESIDENT : best;
   {
     std::lock_guard<std::mutex> lk(g_tuned_mu);
-    g_tuned[TunedKey{g->W, g->H, g->flux_storage}] = best;
+    g_tuned[TunedKey{g->W, g->H, g->flux_storage}] = choice;
   }
-  if (chosen) *chosen = best;
+  if (chosen) *chosen = choice;
   return TWS_OK;
 }
 

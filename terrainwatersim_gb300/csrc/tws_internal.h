@@ -117,6 +117,16 @@ cudaError_t encode_step_maps(int variant, int flux_storage, int W, int H, int pi
                              const float* b, const float* d, const void* f, CUtensorMap* tm_b,
                              CUtensorMap* tm_d, CUtensorMap* tm_f, std::string* why);
 
+// tws_resident.cu: the whole grid in the shared memory of one cluster of up
+// to kResidentMaxCluster CTAs, up to kResidentMaxSteps steps per launch.
+constexpr int kResidentMaxCluster = 16;
+constexpr int kResidentMaxSteps = 4096;
+// cudaSuccess if a W x H grid fits a cluster of `ctas` CTAs (0: the automatic
+// size, returned in *chosen) and the device can run that cluster
+cudaError_t resident_supported(int W, int H, int flux_storage, int ctas, int* chosen);
+cudaError_t launch_resident(int flux_storage, int ctas, const float* b, const float* d,
+                            const void* f, const StepArgs& a, int nsteps, cudaStream_t s);
+
 // tws_aux.cu
 cudaError_t launch_apply_source(float* d, int W, int H, int pitch, const DevSource& s,
                                 cudaStream_t st);

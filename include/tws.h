@@ -204,10 +204,12 @@ TWS_API int tws_test_inject_missing_bytes(tws_grid* grid, int bytes);
  * current state (restored afterwards, so the simulation is unchanged), picks
  * the fastest per cell-step, pins it on this grid and records it for every
  * later grid of the same width, height and flux storage in this process.
- * Where the grid fits the resident kernel (below), that is timed too.
+ * Where the grid fits the resident kernel (below), that is timed too; if it
+ * is fastest, it runs every later tws_step call of at least 16 steps on
+ * grids of this shape, and the fastest tiled variant the shorter calls.
  * Synchronous.  `chosen` (may be NULL) receives the variant index, or
- * TWS_VARIANT_RESIDENT if the resident kernel was fastest (it is then turned
- * on for this grid).  No counterpart in the reference. */
+ * TWS_VARIANT_RESIDENT if the resident kernel was fastest.  No counterpart
+ * in the reference. */
 #define TWS_VARIANT_RESIDENT (-2)
 TWS_API int tws_autotune(tws_grid* grid, int trial_steps, int* chosen);
 

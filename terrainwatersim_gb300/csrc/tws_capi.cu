@@ -158,13 +158,18 @@ struct TunedKey {
     return w != o.w ? w < o.w : (h != o.h ? h < o.h : fs < o.fs);
   }
 };
+// The fastest tiled variant, and whether the resident kernel beat it.
+struct Tuned {
+  int variant = -1;
+  bool resident = false;
+};
 std::mutex g_tuned_mu;
-std::map<TunedKey, int> g_tuned;
+std::map<TunedKey, Tuned> g_tuned;
 
-int tuned_lookup(const tws_grid* g) {
+Tuned tuned_lookup(const tws_grid* g) {
   std::lock_guard<std::mutex> lk(g_tuned_mu);
   auto it = g_tuned.find(TunedKey{g->W, g->H, g->flux_storage});
-  return it == g_tuned.end() ? -1 : it->second;
+  return it == g_tuned.end() ? Tuned{} : it->second;
 }
 
 // Without tuning: two steps per launch (the unified-layout K = 2 tiles, the
@@ -175,19 +180,25 @@ int default_steps_per_launch(const tws_grid* g) { return g->W >= 64 && g->H >= 6
 int chosen_variant(const tws_grid* g) {
   if (g->variant >= 0) return g->variant;
   if (g->steps_per_launch == 0) {
-    const int t = tuned_lookup(g);
-    if (t >= 0) return t;
+    const Tuned t = tuned_lookup(g);
+    if (t.variant >= 0) return t.variant;
   }
   const int k = g->steps_per_launch > 0 ? g->steps_per_launch : default_steps_per_launch(g);
   return step_variant_for(k, g->flux_storage);
 }
 
-// CTAs of the resident kernel if it runs this grid's steps, else 0: it runs
-// them if it was turned on for this grid, or if nothing is pinned and the
-// autotuner chose it for this grid shape (with the automatic cluster size).
-int resident_ctas(const tws_grid* g) {
+// Calls shorter than this keep the tiled kernels when the resident kernel
+// was chosen by the autotuner (whose trials are long calls): one resident
+// launch loads and stores the whole state, which a step or two cannot repay.
+constexpr int kResidentAutoMinSteps = 16;
+
+// CTAs of the resident kernel if it runs a call of `nsteps` steps, else 0:
+// it runs them if it was turned on for this grid, or if nothing is pinned,
+// the autotuner chose it for this grid shape and the call is long enough.
+int resident_ctas(const tws_grid* g, int nsteps) {
   if (g->resident > 0) return g->resident;
-  if (g->variant >= 0 || g->steps_per_launch != 0 || tuned_lookup(g) != TWS_VARIANT_RESIDENT)
+  if (g->variant >= 0 || g->steps_per_launch != 0 || nsteps < kResidentAutoMinSteps ||
+      !tuned_lookup(g).resident)
     return 0;
   int ctas = 0;
   if (resident_supported(g->W, g->H, g->flux_storage, 0, &ctas) != cudaSuccess) {
@@ -219,7 +230,7 @@ StepArgs make_step_args(const tws_grid* g) {
 
 int enqueue_steps(tws_grid* g, int nsteps) {
   StepArgs a = make_step_args(g);
-  if (const int ctas = resident_ctas(g)) {
+  if (const int ctas = resident_ctas(g, nsteps)) {
     for (int left = nsteps; left > 0;) {
       const int n = std::min(left, kResidentMaxSteps);
       const int nxt = g->cur ^ 1;
@@ -677,12 +688,14 @@ TWS_API int tws_autotune(tws_grid* g, int trial_steps, int* chosen) {
     g->resident = saved_resident;
     return rc;
   }
-  g->variant = best;
-  g->resident = resident_best ? res_ctas : 0;
+  // a resident choice is not pinned: it runs the long calls, the fastest
+  // tiled variant the short ones
+  g->variant = resident_best ? -1 : best;
+  g->resident = 0;
   const int choice = resident_best ? TWS_VARIANT_RESIDENT : best;
   {
     std::lock_guard<std::mutex> lk(g_tuned_mu);
-    g_tuned[TunedKey{g->W, g->H, g->flux_storage}] = choice;
+    g_tuned[TunedKey{g->W, g->H, g->flux_storage}] = Tuned{best, resident_best};
   }
   if (chosen) *chosen = choice;
   return TWS_OK;

@@ -50,6 +50,17 @@ TWS_F32X2_OP(fsub2, "sub.rn.f32x2")
 TWS_F32X2_OP(fmul2, "mul.rn.f32x2")
 #undef TWS_F32X2_OP
 
+// F16 storage rounding: the value the next step will read back.
+__device__ __forceinline__ float quantize_f16(float v, float scale, float inv_scale) {
+  const float s = fminf(fmul(v, scale), 65504.0f);
+  return fmul(__half2float(__float2half_rn(s)), inv_scale);
+}
+__device__ __forceinline__ float2 quantize_f16x2(float2 v, float2 scale, float2 inv_scale) {
+  const float2 s = fmul2(v, scale);
+  const __half2 h = __floats2half2_rn(fminf(s.x, 65504.0f), fminf(s.y, 65504.0f));
+  return fmul2(__half22float2(h), inv_scale);
+}
+
 // GLSL clamp(v, 0, 1).
 __device__ __forceinline__ float saturate01(float v) {
   const float m = (v < 0.0f) ? 0.0f : v;

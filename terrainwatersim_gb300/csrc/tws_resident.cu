@@ -50,52 +50,49 @@ __host__ __device__ constexpr size_t res_floats(int R, int W) {
   return (size_t)(7 * R + 4) * W;
 }
 
-__device__ __forceinline__ float quantize_res(float v, float scale, float inv_scale) {
-  const float s = fminf(fmul(v, scale), 65504.0f);
-  return fmul(__half2float(__float2half_rn(s)), inv_scale);
-}
-
 struct ResPlanes {
   float *b, *d, *h, *f0, *f1, *f2, *f3;
   // own row r: b, d, f0, f1, f3 at r * W; h and f2 at (r + 1) * W
 };
 
-// Outflow of one cell, flowUpdate.comp:34-62.
+// Outflow of one cell, flowUpdate.comp:34-62.  Channel pairs in packed
+// f32x2 operations (lane by lane the same IEEE operations); packed products
+// are summed with scalar adds, which the assembler does not contract.
 template <bool F16>
 __device__ __forceinline__ float4 outflow(const ResPlanes& p, const StepArgs& a, int W, int H,
                                           int r, int x, int y) {
   const int i = r * W + x, j = i + W;  // j: the cell in the planes with a ghost row above
   const float hc = p.h[j];
-  const float hx1 = x + 1 < W ? p.h[j + 1] : 0.0f;
-  const float hx0 = x > 0 ? p.h[j - 1] : 0.0f;
-  const float hy1 = p.h[j + W];
-  const float hy0 = p.h[j - W];
+  const float2 hc2 = make_float2(hc, hc);
+  const float2 ex = fsub2(hc2, make_float2(x + 1 < W ? p.h[j + 1] : 0.0f,    // (+x, -x)
+                                           x > 0 ? p.h[j - 1] : 0.0f));
+  const float2 ey = fsub2(hc2, make_float2(p.h[j + W], p.h[j - W]));        // (+y, -y)
   const float dc = p.d[i];
-  float nx = max0(fadd(fmul(p.f0[i], a.kf), fmul(fsub(hc, hx1), a.ka)));
-  float ny = max0(fadd(fmul(p.f1[i], a.kf), fmul(fsub(hc, hx0), a.ka)));
-  float nz = max0(fadd(fmul(p.f2[j], a.kf), fmul(fsub(hc, hy1), a.ka)));
-  float nw = max0(fadd(fmul(p.f3[i], a.kf), fmul(fsub(hc, hy0), a.ka)));
+  const float2 kf2 = make_float2(a.kf, a.kf), ka2 = make_float2(a.ka, a.ka);
+  const float2 px = fmul2(make_float2(p.f0[i], p.f1[i]), kf2), qx = fmul2(ex, ka2);
+  const float2 py = fmul2(make_float2(p.f2[j], p.f3[i]), kf2), qy = fmul2(ey, ka2);
+  float2 nx = make_float2(max0_fast(fadd(px.x, qx.x)), max0_fast(fadd(px.y, qx.y)));
+  float2 ny = make_float2(max0_fast(fadd(py.x, qy.x)), max0_fast(fadd(py.y, qy.y)));
   if (a.closed) {
-    if (x + 1 >= W) nx = 0.0f;
-    if (x == 0) ny = 0.0f;
-    if (y + 1 >= H) nz = 0.0f;
-    if (y == 0) nw = 0.0f;
+    if (x + 1 >= W) nx.x = 0.0f;
+    if (x == 0) nx.y = 0.0f;
+    if (y + 1 >= H) ny.x = 0.0f;
+    if (y == 0) ny.y = 0.0f;
   }
-  const float total = fmul(fadd(fadd(fadd(nx, ny), nz), nw), a.c);
+  const float total = fmul(fadd(fadd(fadd(nx.x, nx.y), ny.x), ny.y), a.c);
   if (total > dc) {
-    const float s = fdiv(dc, total);
-    nx = fmul(nx, s);
-    ny = fmul(ny, s);
-    nz = fmul(nz, s);
-    nw = fmul(nw, s);
+    const float sc = scale_factor(dc, total);
+    const float2 sc2 = make_float2(sc, sc);
+    nx = fmul2(nx, sc2);
+    ny = fmul2(ny, sc2);
   }
   if (F16) {
-    nx = quantize_res(nx, a.flux_scale, a.flux_inv_scale);
-    ny = quantize_res(ny, a.flux_scale, a.flux_inv_scale);
-    nz = quantize_res(nz, a.flux_scale, a.flux_inv_scale);
-    nw = quantize_res(nw, a.flux_scale, a.flux_inv_scale);
+    const float2 fs2 = make_float2(a.flux_scale, a.flux_scale);
+    const float2 fi2 = make_float2(a.flux_inv_scale, a.flux_inv_scale);
+    nx = quantize_f16x2(nx, fs2, fi2);
+    ny = quantize_f16x2(ny, fs2, fi2);
   }
-  return make_float4(nx, ny, nz, nw);
+  return make_float4(nx.x, nx.y, ny.x, ny.y);
 }
 
 __device__ __forceinline__ void store_outflow(const ResPlanes& p, int W, int r, int x,
@@ -107,11 +104,12 @@ __device__ __forceinline__ void store_outflow(const ResPlanes& p, int W, int r, 
   p.f3[i] = n.w;
 }
 
-// Depth and flow vector of one cell, flowApply.comp:32-52.
+// Depth of one cell, flowApply.comp:32-41, with the neighbours' channels it
+// read (the flow vector, lines 45-46, is formed from them on the last step).
 struct Applied {
   float4 fo;
+  float X1, X0, Y1, Y0;
   float d;
-  float2 v;
 };
 
 __device__ __forceinline__ Applied apply(const ResPlanes& p, const StepArgs& a, int W, int r,
@@ -119,15 +117,15 @@ __device__ __forceinline__ Applied apply(const ResPlanes& p, const StepArgs& a, 
   const int i = r * W + x, j = i + W;
   Applied o;
   o.fo = make_float4(p.f0[i], p.f1[i], p.f2[j], p.f3[i]);
-  const float X1 = x + 1 < W ? p.f1[i + 1] : 0.0f;
-  const float X0 = x > 0 ? p.f0[i - 1] : 0.0f;
-  const float Y1 = p.f3[i + W];
-  const float Y0 = p.f2[i];
-  const float in = fadd(fadd(fadd(X1, X0), Y1), Y0);
-  const float out = fadd(fadd(fadd(o.fo.x, o.fo.y), o.fo.z), o.fo.w);
-  o.d = max0(fadd(p.d[i], fmul(fsub(in, out), a.c)));
-  o.v = make_float2(fsub(fsub(X1, o.fo.x), fsub(X0, o.fo.y)),
-                    fsub(fsub(Y1, o.fo.z), fsub(Y0, o.fo.w)));
+  o.X1 = x + 1 < W ? p.f1[i + 1] : 0.0f;  // -x outflow of the +x neighbour
+  o.X0 = x > 0 ? p.f0[i - 1] : 0.0f;      // +x outflow of the -x neighbour
+  o.Y1 = p.f3[i + W];                     // -y outflow of the +y neighbour
+  o.Y0 = p.f2[i];                         // +y outflow of the -y neighbour
+  // (inflow, outflow) side by side, each in the shader's order
+  float2 io = fadd2(make_float2(o.X1, o.fo.x), make_float2(o.X0, o.fo.y));
+  io = fadd2(io, make_float2(o.Y1, o.fo.z));
+  io = fadd2(io, make_float2(o.Y0, o.fo.w));
+  o.d = max0_fast(fadd(p.d[i], fmul(fsub(io.x, io.y), a.c)));
   return o;
 }
 
@@ -270,10 +268,9 @@ __global__ void __launch_bounds__(kResThreads, 1)
         const size_t g = (size_t)y * pitch + x;
         a.d_out[g] = o.d;
         if (F16) {
-          const __half2 lo =
-              __floats2half2_rn(fmul(o.fo.x, a.flux_scale), fmul(o.fo.y, a.flux_scale));
-          const __half2 hi =
-              __floats2half2_rn(fmul(o.fo.z, a.flux_scale), fmul(o.fo.w, a.flux_scale));
+          const float2 fs2 = make_float2(a.flux_scale, a.flux_scale);
+          const __half2 lo = __float22half2_rn(fmul2(make_float2(o.fo.x, o.fo.y), fs2));
+          const __half2 hi = __float22half2_rn(fmul2(make_float2(o.fo.z, o.fo.w), fs2));
           uint2 packed;
           packed.x = *reinterpret_cast<const uint32_t*>(&lo);
           packed.y = *reinterpret_cast<const uint32_t*>(&hi);
@@ -281,7 +278,8 @@ __global__ void __launch_bounds__(kResThreads, 1)
         } else {
           reinterpret_cast<float4*>(a.f_out)[g] = o.fo;
         }
-        a.v_out[g] = o.v;
+        a.v_out[g] = fsub2(fsub2(make_float2(o.X1, o.Y1), make_float2(o.fo.x, o.fo.z)),
+                           fsub2(make_float2(o.X0, o.Y0), make_float2(o.fo.y, o.fo.w)));
       } else {
         const int i = rr * W + x;
         const float d = sources(o.d, x, y);

@@ -167,17 +167,6 @@ struct Tile {
   static constexpr uint32_t TX_BYTES = (uint32_t)(2 * NB * 4 + (F16 ? SW * FH * 8 : NF * 16));
 };
 
-// F16 storage rounding: the value the next step will read back.
-__device__ __forceinline__ float quantize_f16(float v, float scale, float inv_scale) {
-  const float s = fminf(fmul(v, scale), 65504.0f);
-  return fmul(__half2float(__float2half_rn(s)), inv_scale);
-}
-__device__ __forceinline__ float2 quantize_f16x2(float2 v, float2 scale, float2 inv_scale) {
-  const float2 s = fmul2(v, scale);
-  const __half2 h = __floats2half2_rn(fminf(s.x, 65504.0f), fminf(s.y, 65504.0f));
-  return fmul2(__half22float2(h), inv_scale);
-}
-
 // The three TMA loads of the tile at (x0, y0) into one stage buffer.
 // `missing` (normally 0) is the test hook of tws_test_inject_missing_bytes:
 // the barrier then expects bytes that never arrive and its wait runs out.

@@ -196,6 +196,16 @@ def test_autotune_considers_it_and_keeps_state(tws, oracle):
         assert best == tws.VARIANT_RESIDENT or 0 <= best < len(tws.variants())
         g.step(7)
         gd, gf, gv = g.download()
+        if best == tws.VARIANT_RESIDENT:
+            # long calls take one resident launch, short ones the tiled kernels
+            n0 = tws.lib().tws_launch_count()
+            g.step(40)
+            g.sync()
+            assert tws.lib().tws_launch_count() - n0 == 1
+            n0 = tws.lib().tws_launch_count()
+            g.step(1)
+            g.sync()
+            assert tws.lib().tws_launch_count() - n0 == 1
     od, of, ov = oracle_run(oracle, b, d, np.zeros((H, W, 4), np.float32), p.as_tuple(), rain, 12,
                             oracle.BOUNDARY_CLOSED)
     assert_bitexact(gd, od, "depth")

@@ -67,7 +67,8 @@ def test_c1_configuration_bitexact(tws, oracle):
     assert_bitexact(gv, ov, "velocity")
 
 
-@pytest.mark.parametrize("W,H", [(97, 130), (300, 41), (33, 17), (1, 70), (70, 1), (5, 3)])
+@pytest.mark.parametrize("W,H", [(97, 130), (300, 41), (600, 40), (33, 17), (1, 70), (70, 1),
+                                 (5, 3)])
 @pytest.mark.parametrize("boundary", [0, 1])
 def test_shapes_and_boundaries_bitexact(tws, oracle, W, H, boundary):
     """Row splits that leave the last CTAs with fewer or no rows, single rows

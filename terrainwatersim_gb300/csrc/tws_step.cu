@@ -55,6 +55,17 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 __device__ __forceinline__ void fence_mbar_init() {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
+// Programmatic dependent launch.  A step launch may be scheduled while the
+// previous launch on the stream is still finishing; it waits here, before
+// its first global-memory access, until that launch has completed and its
+// writes are visible (a hardware wait that ends when the previous grid does).
+// Having passed it, the CTA lets the next launch be scheduled in turn.
+__device__ __forceinline__ void wait_previous_launch() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+__device__ __forceinline__ void allow_next_launch() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
 // Orders this thread's view of earlier generic-proxy shared-memory accesses
 // (made visible to it by __syncthreads) before a following TMA write.
 __device__ __forceinline__ void fence_proxy_async_smem() {
@@ -621,6 +632,8 @@ __global__ void __launch_bounds__(kThreads)
     fence_mbar_init();
   }
   __syncthreads();
+  wait_previous_launch();
+  allow_next_launch();
   if (tid == 0) {
 #pragma unroll
     for (int s = 0; s < STAGES; ++s) {
@@ -729,6 +742,10 @@ __global__ void __launch_bounds__(kThreads, MINB)
                              : reinterpret_cast<float4*>(smem + T::ST_F);
   const int tid = threadIdx.x;
   const StepArgs& a = G.a;
+  // the unit and grid tables are written before the chain, the state by the
+  // previous launch: wait for it before the tile load
+  wait_previous_launch();
+  allow_next_launch();
   if (tid == 0) {
     mbar_init(bar, 1);
     fence_mbar_init();
@@ -1001,9 +1018,21 @@ cudaError_t launch_step(int variant, int flux_storage, const CUtensorMap* tm_b,
   }
   if (grid.y > 65535) return cudaErrorInvalidConfiguration;
   auto kfn = reinterpret_cast<KernelFn>(const_cast<void*>(fn));
-  kfn<<<grid, kThreads, smem, s>>>(*tm_b, *tm_d, *tm_f, a);
+  // programmatic dependent launch: the kernel waits for the previous launch
+  // before it touches global memory (wait_previous_launch)
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(kThreads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const cudaError_t launched = cudaLaunchKernelEx(&cfg, kfn, *tm_b, *tm_d, *tm_f, a);
   count_launch();
-  return cudaGetLastError();
+  return launched;
 }
 
 // ---- batched variants ---------------------------------------------------------
@@ -1102,9 +1131,20 @@ cudaError_t launch_batch_step(int variant, int flux_storage, const BatchGrid* gr
   const int fs = flux_storage == TWS_FLUX_F16 ? TWS_FLUX_F16 : TWS_FLUX_F32;
   BatchEntry& e = batch_table().e[variant];
   auto fn = reinterpret_cast<BatchFn>(const_cast<void*>(e.fn[fs]));
-  fn<<<blocks, kThreads, e.smem[fs], s>>>(grids, units, launch_idx);
+  // programmatic dependent launch, as for the single-grid step kernels
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3((unsigned)blocks, 1, 1);
+  cfg.blockDim = dim3(kThreads, 1, 1);
+  cfg.dynamicSmemBytes = e.smem[fs];
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const cudaError_t launched = cudaLaunchKernelEx(&cfg, fn, grids, units, launch_idx);
   count_launch();
-  return cudaGetLastError();
+  return launched;
 }
 
 }  // namespace tws

@@ -79,6 +79,23 @@ def test_invalid_arguments_rejected_without_touching_the_gpu(tws):
     bad = tws.SimParams(0.998, 0.1962, 0.02, 1.0, 9)
     assert L.tws_create(16, 16, C.byref(bad), 0, None, C.byref(h)) == tws.ERR_INVALID
     assert L.tws_error_string(tws.ERR_TIMEOUT) == b"device-side wait timed out"
+    # asynchronous host I/O and the resident kernel: null handles
+    assert L.tws_upload_async(None, None, None, None) == tws.ERR_INVALID
+    assert L.tws_download_async(None, None, None, None) == tws.ERR_INVALID
+    assert L.tws_io_wait(None) == tws.ERR_INVALID
+    assert L.tws_set_resident(None, tws.RESIDENT_AUTO) == tws.ERR_INVALID
+    assert L.tws_resident_fits(64, 64, 7) == 0  # no such flux storage
+
+
+def test_resident_fits_answers_no_without_a_gpu(tws):
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    assert tws.resident_fits(256, 256) == 0
+    assert tws.resident_fits(0, 0) == 0
 
 
 def test_no_cpu_fallback(tws):

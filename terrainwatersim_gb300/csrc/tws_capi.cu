@@ -48,6 +48,7 @@ struct tws_grid {
   int steps_per_launch = 0;  // 0: library's choice
   int variant = -1;          // pinned kernel variant, -1: automatic
   int resident = 0;          // > 0: the resident kernel runs the steps, on this many CTAs
+  int auto_ctas = -1;        // the resident kernel's automatic cluster for this grid (-1: not asked yet)
   std::vector<VariantMaps> maps;
   tws_source src[TWS_MAX_SOURCES];
   int nsrc = 0;
@@ -195,17 +196,20 @@ constexpr int kResidentAutoMinSteps = 16;
 // CTAs of the resident kernel if it runs a call of `nsteps` steps, else 0:
 // it runs them if it was turned on for this grid, or if nothing is pinned,
 // the autotuner chose it for this grid shape and the call is long enough.
-int resident_ctas(const tws_grid* g, int nsteps) {
+int resident_ctas(tws_grid* g, int nsteps) {
   if (g->resident > 0) return g->resident;
   if (g->variant >= 0 || g->steps_per_launch != 0 || nsteps < kResidentAutoMinSteps ||
       !tuned_lookup(g).resident)
     return 0;
-  int ctas = 0;
-  if (resident_supported(g->W, g->H, g->flux_storage, 0, &ctas) != cudaSuccess) {
-    cudaGetLastError();
-    return 0;
+  if (g->auto_ctas < 0) {  // asked once per grid
+    int ctas = 0;
+    if (resident_supported(g->W, g->H, g->flux_storage, 0, &ctas) != cudaSuccess) {
+      cudaGetLastError();
+      ctas = 0;
+    }
+    g->auto_ctas = ctas;
   }
-  return ctas;
+  return g->auto_ctas;
 }
 
 StepArgs make_step_args(const tws_grid* g) {

@@ -212,3 +212,34 @@ def test_autotune_considers_it_and_keeps_state(tws, oracle):
     assert_bitexact(gd, od, "depth")
     assert_bitexact(gf, of, "flux")
     assert_bitexact(gv, ov, "velocity")
+
+
+def test_reference_scene_with_pipelined_io(tws, oracle):
+    """The reference's own noise scene (open border, the reference's brush
+    parameters), advanced by the resident kernel in calls of 100 steps while
+    each state is downloaded asynchronously: every download is the oracle's
+    state after that many steps."""
+    import torch
+    W = H = 192
+    p = tws.params_reference(60.0, 0.98, 10.0, 1024.0, W, tws.BOUNDARY_OPEN)
+    brush = [(tws.SOURCE_BRUSH, 100.5, 80.25, 32.0, 0.5)]
+    outs = [tuple(torch.empty(shape, dtype=torch.float32, pin_memory=True).numpy()
+                  for shape in ((H, W), (H, W, 4), (H, W, 2))) for _ in range(3)]
+    with tws.Grid(W, H, p) as g:
+        g.generate_reference_scene()
+        g.set_sources(brush)
+        g.set_resident(True)
+        for i in range(3):
+            g.step(100)
+            g.download_async(outs[i])
+        g.io_wait()
+    b, d = oracle.reference_terrain(W, H)
+    f = np.zeros((H, W, 4), np.float32)
+    v = np.zeros((H, W, 2), np.float32)
+    kf, ka, c = p.as_tuple()
+    for i in range(3):
+        oracle.step_f32(b, d, f, v, kf, ka, c, oracle.BOUNDARY_OPEN,
+                        [(s[0], s[1], s[2], s[3], s[4]) for s in brush], nsteps=100)
+        assert_bitexact(outs[i][0], d, f"depth after {100 * (i + 1)} steps")
+        assert_bitexact(outs[i][1], f, f"flux after {100 * (i + 1)} steps")
+        assert_bitexact(outs[i][2], v, f"velocity after {100 * (i + 1)} steps")

@@ -158,3 +158,68 @@ def test_async_rejects_bad_arguments(tws):
             g.download_async((np.empty((32, 31), np.float32), None, None))
         assert tws.lib().tws_upload_async(g.handle, None, None, None) == tws.ERR_INVALID
     assert tws.lib().tws_io_wait(None) == tws.ERR_INVALID
+
+
+def test_async_io_on_batch_members(tws, oracle):
+    """Grids of a batch take asynchronous uploads and downloads on the
+    batch's stream order: each result is its own grid's oracle state."""
+    sizes = [(96, 64), (130, 70), (64, 160)]
+    p = tws.params_physical(0.02, 9.81, 1.0, 1.0, 0.998, tws.BOUNDARY_CLOSED)
+    grids, inputs, outs = [], [], []
+    with tws.Batch() as batch:
+        for k, (W, H) in enumerate(sizes):
+            b, d, f = scene(oracle, tws, 40 + k, W, H)
+            g = tws.Grid(W, H, p)
+            g.set_sources(tws.rain_disks(40 + k, W, H, 6, 0.01, 1))
+            batch.add(g)
+            g.upload_async(b, d, f)
+            grids.append(g)
+            inputs.append((b, d, f))
+            outs.append((pinned((H, W)), pinned((H, W, 4)), pinned((H, W, 2))))
+        batch.step(24)
+        for g, o in zip(grids, outs):
+            g.download_async(o)
+        for g in grids:
+            g.io_wait()
+        batch.sync()
+        for g in grids:
+            batch.remove(g)
+    for k, (W, H) in enumerate(sizes):
+        rain = tws.rain_disks(40 + k, W, H, 6, 0.01, 1)
+        od, of, ov = oracle_state(oracle, *inputs[k], p.as_tuple(), rain, 24)
+        assert_bitexact(outs[k][0], od, f"depth grid {k}")
+        assert_bitexact(outs[k][1], of, f"flux grid {k}")
+        assert_bitexact(outs[k][2], ov, f"velocity grid {k}")
+    for g in grids:
+        g.close()
+
+
+def test_timeout_during_pipelined_io_is_reported_and_recovers(tws, oracle):
+    """A tile load that never completes (the test hook) inside a pipelined
+    upload / steps / download sequence: the copies still finish, tws_sync
+    reports the time-out once, and the next pipelined round trip is exact."""
+    W, H = 96, 64
+    p = tws.params_physical(0.02, 9.81, 1.0, 1.0, 0.998, tws.BOUNDARY_CLOSED)
+    b, d, f = scene(oracle, tws, 61, W, H)
+    out = (pinned((H, W)), pinned((H, W, 4)), pinned((H, W, 2)))
+    with tws.Grid(W, H, p) as g:
+        g.set_steps_per_launch(2)
+        g.set_wait_limit(2_000_000)
+        g.test_inject_missing_bytes(16)
+        g.upload_async(b, d, f)
+        g.step(4)
+        g.download_async(out)
+        g.io_wait()
+        with pytest.raises(tws.TwsError) as e:
+            g.sync()
+        assert e.value.code == tws.ERR_TIMEOUT
+        g.sync()  # reported once
+        g.test_inject_missing_bytes(0)
+        g.upload_async(b, d, f)
+        g.step(6)
+        g.download_async(out)
+        g.sync()
+    od, of, ov = oracle_state(oracle, b, d, f, p.as_tuple(), [], 6)
+    assert_bitexact(out[0], od, "depth")
+    assert_bitexact(out[1], of, "flux")
+    assert_bitexact(out[2], ov, "velocity")

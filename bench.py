@@ -419,10 +419,12 @@ def cpu_baseline_leg(tws, g, size, budget_s):
     src = [(s[0], s[1], s[2], s[3], s[4]) for s in rain]
     kf, ka, c = p.as_tuple()
     threads = O.max_threads()
-    t1 = O.step_f32(b, d, f, v, kf, ka, c, O.BOUNDARY_CLOSED, src, nsteps=1, threads=threads)
-    n = int(max(1, min(400, budget_s / max(t1, 1e-6))))
+    # one step touches the pages, four more size the sample to about budget_s
+    O.step_f32(b, d, f, v, kf, ka, c, O.BOUNDARY_CLOSED, src, nsteps=1, threads=threads)
+    t4 = O.step_f32(b, d, f, v, kf, ka, c, O.BOUNDARY_CLOSED, src, nsteps=4, threads=threads)
+    n = int(max(1, min(4000, budget_s / max(t4 / 4, 1e-6))))
     tn = O.step_f32(b, d, f, v, kf, ka, c, O.BOUNDARY_CLOSED, src, nsteps=n, threads=threads)
-    total_steps = n + 1
+    total_steps = n + 5
     # the GPU on the same steps
     g.generate_scene(2026, 40.0, 15.0)
     g.set_sources(rain)
@@ -434,12 +436,23 @@ def cpu_baseline_leg(tws, g, size, budget_s):
                     and np.array_equal(gf.view(np.uint32), f.view(np.uint32))
                     and np.array_equal(gv.view(np.uint32), v.view(np.uint32)))
     vg, vo = float(np.sum(gd, dtype=np.float64)), O.volume(d)
+    # the FP64 oracle on a few steps of the same grid (reported beside the FP32 port)
+    b64, d64 = (a.astype(np.float64) for a in O.terrain(2026, size, size, 40.0, 15.0))
+    f64 = np.zeros((size, size, 4), np.float64)
+    k64 = O.params_physical()
+    src64 = [(s[0], s[1], s[2], s[3], 0.01) for s in rain]
+    O.step_f64(b64, d64, f64, None, *k64, O.BOUNDARY_CLOSED, src64, nsteps=1, threads=threads)
+    n64 = max(1, min(n, 20))
+    t64 = O.step_f64(b64, d64, f64, None, *k64, O.BOUNDARY_CLOSED, src64, nsteps=n64,
+                     threads=threads)
     return {
         "value": round(size * size * n / tn / 1e9, 4),
+        "fp64_value": round(size * size * n64 / t64 / 1e9, 4),
+        "fp64_sample": f"FP64 oracle, {n64} steps of the same grid (+1 warm-up step)",
         "unit": "Gcell-steps/s",
         "cores": threads,
         "kind": "port",
-        "sample": f"{size}x{size} grid, {n} steps timed (+1 warm-up step), FP32 oracle, "
+        "sample": f"{size}x{size} grid, {n} steps timed (+5 warm-up steps), FP32 oracle, "
                   f"OpenMP {threads} threads; GPU state after the same {total_steps} steps "
                   "compared on the full grid",
         "seconds": round(tn, 3),
@@ -554,13 +567,17 @@ def run_c1(args):
     ov = np.zeros((H, W, 2), np.float32)
     src = [(s[0], s[1], s[2], s[3], s[4]) for s in rain]
     kf, ka, c = p.as_tuple()
-    O.step_f32(b, od, of, ov, kf, ka, c, O.BOUNDARY_CLOSED, src, nsteps=steps)
+    threads = O.max_threads()
+    # the oracle's own step loops are the timed CPU baseline (FP32 and FP64)
+    t32 = O.step_f32(b, od, of, ov, kf, ka, c, O.BOUNDARY_CLOSED, src, nsteps=steps,
+                     threads=threads)
     b64, d64 = O.terrain(2026, W, H, 40.0, 15.0)
     b64, d64 = b64.astype(np.float64), d64.astype(np.float64)
     f64 = np.zeros((H, W, 4), np.float64)
     k64 = O.params_physical()
-    O.step_f64(b64, d64, f64, None, *k64, O.BOUNDARY_CLOSED,
-               [(s[0], s[1], s[2], s[3], 0.01) for s in rain], nsteps=steps)
+    t64 = O.step_f64(b64, d64, f64, None, *k64, O.BOUNDARY_CLOSED,
+                     [(s[0], s[1], s[2], s[3], 0.01) for s in rain], nsteps=steps,
+                     threads=threads)
     v64 = O.volume(d64)
     g.close()
     resident = None
@@ -605,6 +622,10 @@ def run_c1(args):
         "max_abs_depth_err_vs_fp64": float(np.abs(d - d64).max()),
         "rel_volume_drift_vs_fp64": abs(vol - v64) / v64,
         "resident": resident,
+        "cpu_oracle": {"fp32_gcell_steps_per_s": round(W * H * steps / t32 / 1e9, 4),
+                       "fp64_gcell_steps_per_s": round(W * H * steps / t64 / 1e9, 4),
+                       "cores": threads, "kind": "port",
+                       "sample": f"the same {steps} steps of the {W}x{H} grid, OpenMP"},
     }
 
 

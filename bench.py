@@ -419,12 +419,15 @@ def cpu_baseline_leg(tws, g, size, budget_s):
     src = [(s[0], s[1], s[2], s[3], s[4]) for s in rain]
     kf, ka, c = p.as_tuple()
     threads = O.max_threads()
-    # one step touches the pages, four more size the sample to about budget_s
+    # one step touches the pages, four more size the sample to about budget_s,
+    # timed as three runs of n steps that continue the same state (median)
     O.step_f32(b, d, f, v, kf, ka, c, O.BOUNDARY_CLOSED, src, nsteps=1, threads=threads)
     t4 = O.step_f32(b, d, f, v, kf, ka, c, O.BOUNDARY_CLOSED, src, nsteps=4, threads=threads)
-    n = int(max(1, min(4000, budget_s / max(t4 / 4, 1e-6))))
-    tn = O.step_f32(b, d, f, v, kf, ka, c, O.BOUNDARY_CLOSED, src, nsteps=n, threads=threads)
-    total_steps = n + 5
+    n = int(max(1, min(2000, budget_s / 3 / max(t4 / 4, 1e-6))))
+    runs = [O.step_f32(b, d, f, v, kf, ka, c, O.BOUNDARY_CLOSED, src, nsteps=n, threads=threads)
+            for _ in range(3)]
+    tn = statistics.median(runs)
+    total_steps = 3 * n + 5
     # the GPU on the same steps
     g.generate_scene(2026, 40.0, 15.0)
     g.set_sources(rain)
@@ -442,20 +445,23 @@ def cpu_baseline_leg(tws, g, size, budget_s):
     k64 = O.params_physical()
     src64 = [(s[0], s[1], s[2], s[3], 0.01) for s in rain]
     O.step_f64(b64, d64, f64, None, *k64, O.BOUNDARY_CLOSED, src64, nsteps=1, threads=threads)
-    n64 = max(1, min(n, 20))
-    t64 = O.step_f64(b64, d64, f64, None, *k64, O.BOUNDARY_CLOSED, src64, nsteps=n64,
-                     threads=threads)
+    n64 = max(1, min(n, 10))
+    t64 = statistics.median(
+        O.step_f64(b64, d64, f64, None, *k64, O.BOUNDARY_CLOSED, src64, nsteps=n64,
+                   threads=threads) for _ in range(3))
     return {
         "value": round(size * size * n / tn / 1e9, 4),
         "fp64_value": round(size * size * n64 / t64 / 1e9, 4),
-        "fp64_sample": f"FP64 oracle, {n64} steps of the same grid (+1 warm-up step)",
+        "fp64_sample": f"FP64 oracle, median of 3 runs of {n64} steps of the same grid "
+                       "(+1 warm-up step)",
         "unit": "Gcell-steps/s",
         "cores": threads,
         "kind": "port",
-        "sample": f"{size}x{size} grid, {n} steps timed (+5 warm-up steps), FP32 oracle, "
-                  f"OpenMP {threads} threads; GPU state after the same {total_steps} steps "
-                  "compared on the full grid",
+        "sample": f"{size}x{size} grid, median of 3 runs of {n} steps (+5 warm-up steps), "
+                  f"FP32 oracle, OpenMP {threads} threads; GPU state after the same "
+                  f"{total_steps} steps compared on the full grid",
         "seconds": round(tn, 3),
+        "runs_seconds": [round(t, 3) for t in runs],
         "parity": {"steps": total_steps, "bitexact": bitexact, "max_abs_depth_err": err,
                    "rel_max_depth_err": rel,
                    "rel_volume_diff": abs(vg - vo) / max(1e-30, abs(vo))},
@@ -568,16 +574,25 @@ def run_c1(args):
     src = [(s[0], s[1], s[2], s[3], s[4]) for s in rain]
     kf, ka, c = p.as_tuple()
     threads = O.max_threads()
-    # the oracle's own step loops are the timed CPU baseline (FP32 and FP64)
-    t32 = O.step_f32(b, od, of, ov, kf, ka, c, O.BOUNDARY_CLOSED, src, nsteps=steps,
-                     threads=threads)
-    b64, d64 = O.terrain(2026, W, H, 40.0, 15.0)
-    b64, d64 = b64.astype(np.float64), d64.astype(np.float64)
-    f64 = np.zeros((H, W, 4), np.float64)
+    # the oracle's own step loops are the timed CPU baseline (FP32 and FP64),
+    # each the median of three runs from the initial state
+    d0 = od.copy()
+    t32s = []
+    for _ in range(3):
+        od[...], of[...], ov[...] = d0, 0.0, 0.0
+        t32s.append(O.step_f32(b, od, of, ov, kf, ka, c, O.BOUNDARY_CLOSED, src, nsteps=steps,
+                               threads=threads))
+    t32 = statistics.median(t32s)
     k64 = O.params_physical()
-    t64 = O.step_f64(b64, d64, f64, None, *k64, O.BOUNDARY_CLOSED,
-                     [(s[0], s[1], s[2], s[3], 0.01) for s in rain], nsteps=steps,
-                     threads=threads)
+    t64s = []
+    for _ in range(3):
+        b64, d64 = O.terrain(2026, W, H, 40.0, 15.0)
+        b64, d64 = b64.astype(np.float64), d64.astype(np.float64)
+        f64 = np.zeros((H, W, 4), np.float64)
+        t64s.append(O.step_f64(b64, d64, f64, None, *k64, O.BOUNDARY_CLOSED,
+                               [(s[0], s[1], s[2], s[3], 0.01) for s in rain], nsteps=steps,
+                               threads=threads))
+    t64 = statistics.median(t64s)
     v64 = O.volume(d64)
     g.close()
     resident = None
@@ -625,7 +640,8 @@ def run_c1(args):
         "cpu_oracle": {"fp32_gcell_steps_per_s": round(W * H * steps / t32 / 1e9, 4),
                        "fp64_gcell_steps_per_s": round(W * H * steps / t64 / 1e9, 4),
                        "cores": threads, "kind": "port",
-                       "sample": f"the same {steps} steps of the {W}x{H} grid, OpenMP"},
+                       "sample": f"the same {steps} steps of the {W}x{H} grid, OpenMP, "
+                                 "median of 3 runs"},
     }
 
 

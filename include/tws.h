@@ -116,7 +116,10 @@ typedef struct tws_buffers {
  * 1 <= width <= 2^20, 1 <= height <= 2^19. */
 TWS_API int tws_create(int width, int height, const tws_sim_params* params, int flux_storage,
                        void* stream, tws_grid** out);
-/* Replaces Terrain::~Terrain (Terrain.cpp:134-148). */
+/* Replaces Terrain::~Terrain (Terrain.cpp:134-148).  Waits for the grid's
+ * asynchronous host copies (tws_upload_async / tws_download_async), which may
+ * still read or write caller arrays; device memory returns to the pool in
+ * stream order, without waiting for queued steps. */
 TWS_API int tws_destroy(tws_grid* grid);
 
 /* Reset from host arrays: terrain (required), depth (NULL -> 0), flux

@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--flux", choices=["f32", "f16"], default="f32")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-renderer", action="store_true",
+                    help="skip timing the renderer-facing outputs")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--config", choices=["c1", "c2", "c3", "c4", "c5"], default="c2",
                     help="c2 (default): the 4096^2 headline; c1: 256^2; c3: 64 uneven grids "
@@ -398,6 +400,8 @@ def run_ours(args):
             "gpu_launches": int(launches),
             "clocks": clocks,
         }
+        if not args.no_renderer:
+            result["renderer"] = renderer_leg(tws, torch, g, stream, size, peak)
         if ws == 1 and not args.no_cpu:
             result["cpu_baseline"] = cpu_baseline_leg(tws, g, size, args.cpu_seconds)
     g.close()
@@ -405,6 +409,69 @@ def run_ours(args):
         dist.barrier()
         dist.destroy_process_group()
     return result
+
+
+# Algorithmic bytes per cell of the renderer-facing calls.
+#   surface: read b, d, v (16); write height, render height, flow speed, foam
+#            (4 each), normal (12), dry mask (1)
+#   export:  flow map (read v 8, write 2 halves 4) + TerrainData RGBA32F (read b, d 8,
+#            write 16); its mip pyramid adds, per level l >= 1, the read of level
+#            l - 1 and the write of level l: 16 (4/3 + 1/3) bytes per cell in all
+SURFACE_BYTES_PER_CELL = 45.0
+EXPORT_BYTES_PER_CELL = 36.0
+MIPS_BYTES_PER_CELL = 16.0 * (4.0 / 3.0 + 1.0 / 3.0)
+
+
+def renderer_leg(tws, torch, g, stream, size, peak):
+    """The renderer-facing outputs on the benchmark grid's state: tws_surface and
+    tws_export_textures (with and without the full mip pyramid), each timed with
+    CUDA events on the grid's stream over 20 calls after 3 warm-up calls.  Their
+    inputs (268 MB) and outputs exceed the L2."""
+    cells = size * size
+    dev = torch.device("cuda")
+    f32 = lambda n: torch.empty(n, dtype=torch.float32, device=dev)  # noqa: E731
+    height, rheight, speed, foam = f32(cells), f32(cells), f32(cells), f32(cells)
+    normal = f32(3 * cells)
+    dry = torch.empty(cells, dtype=torch.uint8, device=dev)
+    so = tws.SurfaceOut(height.data_ptr(), rheight.data_ptr(), normal.data_ptr(),
+                        speed.data_ptr(), foam.data_ptr(), dry.data_ptr())
+    rgba = f32(4 * cells)
+    flowmap = torch.empty(2 * cells, dtype=torch.int16, device=dev)
+    levels, texels, w = 0, 0, size
+    while w >= 2:
+        w //= 2
+        levels += 1
+        texels += w * w
+    mips = f32(4 * texels)
+
+    def timed(fn, reps=20, warm=3):
+        for _ in range(warm):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / reps
+
+    def entry(seconds, bpc):
+        gbs = bpc * cells / seconds / 1e9
+        return {"us": round(seconds * 1e6, 2), "bytes_per_cell": round(bpc, 2),
+                "gbs": round(gbs, 1), "frac_of_measured_hbm": round(gbs / peak, 4)}
+
+    t_surface = timed(lambda: g.surface(so))
+    t_export = timed(lambda: g.export_textures(rgba.data_ptr(), flowmap.data_ptr(), 0, None))
+    t_mips = timed(lambda: g.export_textures(rgba.data_ptr(), flowmap.data_ptr(), levels,
+                                             mips.data_ptr()))
+    return {
+        "grid": [size, size],
+        "surface": entry(t_surface, SURFACE_BYTES_PER_CELL),
+        "export": entry(t_export, EXPORT_BYTES_PER_CELL),
+        "export_with_mips": dict(entry(t_mips, EXPORT_BYTES_PER_CELL + MIPS_BYTES_PER_CELL),
+                                 mip_levels=levels),
+    }
 
 
 def cpu_baseline_leg(tws, g, size, budget_s):

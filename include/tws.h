@@ -267,7 +267,8 @@ TWS_API int tws_volume(tws_grid* grid, double* out);
  * partial sums (every partial is rewritten, nothing needs clearing), so two
  * calls that can run on the GPU at the same time -- on different streams,
  * or from different host threads -- race and may return wrong sums:
- * serialise them (one stream, or events). */
+ * serialise them (one stream, or events).  `depth` must be 4-byte and `out`
+ * 8-byte aligned (TWS_ERR_INVALID otherwise). */
 #define TWS_VOLUME_NOALLOC_MAX_ROWS 16384
 TWS_API int tws_volume_noalloc(const float* depth, int width, int height, int pitch,
                                double cell_area, double* out, void* stream);
@@ -278,7 +279,9 @@ TWS_API int tws_volume_noalloc(const float* depth, int width, int height, int pi
  * NULL).  Replaces the reads of TerrainInfo and FlowMap in
  * waterRender.vert:21-23, waterRender.eval:32-35 and waterRender.frag:50-62,
  * 217, 240-241, 341-346 (neighbours wrap around, as the REPEAT sampler bound
- * in Terrain.cpp:313 does).  Asynchronous on the grid's stream. */
+ * in Terrain.cpp:313 does).  The float outputs must be 4-byte aligned
+ * (TWS_ERR_INVALID otherwise); 16-byte aligned outputs and a width that is a
+ * multiple of 4 take a faster path.  Asynchronous on the grid's stream. */
 typedef struct tws_surface_out {
   float* height;        /* d + b                                        */
   float* render_height; /* (d + b) - 0.1, and 10 lower where d < 0.1    */
@@ -296,7 +299,8 @@ TWS_API int tws_surface(tws_grid* grid, const tws_surface_out* out);
  * pyramid of TerrainData (Terrain.cpp:273-276), packed level after level in
  * `mips` (level l is floor(W/2^l) x floor(H/2^l) RGBA32F texels; every level
  * must be at least 1 x 1).  Any pointer may be NULL (mips need terrain_rgba).
- * Asynchronous on the grid's stream. */
+ * terrain_rgba and mips must be 16-byte aligned and flowmap_rg16f 4-byte
+ * aligned (TWS_ERR_INVALID otherwise).  Asynchronous on the grid's stream. */
 TWS_API int tws_export_textures(tws_grid* grid, float* terrain_rgba, uint16_t* flowmap_rg16f,
                                 int mip_levels, float* mips);
 

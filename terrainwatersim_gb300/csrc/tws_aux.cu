@@ -488,6 +488,10 @@ cudaError_t noalloc_scratch(double** out) {
 extern "C" TWS_API int tws_volume_noalloc(const float* depth, int width, int height, int pitch,
                                           double cell_area, double* out, void* stream) {
   if (!depth || !out || width < 1 || height < 1 || pitch < width) return TWS_ERR_INVALID;
+  // the kernels read floats and write a double: natural alignment
+  if (reinterpret_cast<uintptr_t>(depth) % alignof(float) != 0 ||
+      reinterpret_cast<uintptr_t>(out) % alignof(double) != 0)
+    return TWS_ERR_INVALID;
   if (height > TWS_VOLUME_NOALLOC_MAX_ROWS) return TWS_ERR_TOO_LARGE;
   double* scratch = nullptr;
   if (noalloc_scratch(&scratch) != cudaSuccess) return TWS_ERR_CUDA;

@@ -925,6 +925,11 @@ TWS_API int tws_io_wait(tws_grid* g) {
 
 TWS_API int tws_surface(tws_grid* g, const tws_surface_out* o) {
   if (!g || !o) return fail(g, TWS_ERR_INVALID, "null surface output");
+  // the float outputs are written as floats at least: natural alignment
+  for (const void* p : {(const void*)o->height, (const void*)o->render_height,
+                        (const void*)o->normal, (const void*)o->flow_speed, (const void*)o->foam})
+    if (reinterpret_cast<uintptr_t>(p) % 4 != 0)
+      return fail(g, TWS_ERR_INVALID, "surface outputs must be 4-byte aligned");
   TWS_CUDA(g, launch_surface(g->b, g->d[g->cur], g->v, g->W, g->H, g->pitch, *o, g->stream),
            "surface kernel");
   return TWS_OK;
@@ -935,6 +940,12 @@ TWS_API int tws_export_textures(tws_grid* g, float* terrain_rgba, uint16_t* flow
   if (!g || mip_levels < 0) return fail(g, TWS_ERR_INVALID, "bad export arguments");
   if (mip_levels > 0 && (!terrain_rgba || !mips))
     return fail(g, TWS_ERR_INVALID, "mips need terrain_rgba and mips buffers");
+  // RGBA32F texels are moved as 16-byte vectors, RG16F texels as 4-byte pairs
+  if (reinterpret_cast<uintptr_t>(terrain_rgba) % 16 != 0 ||
+      reinterpret_cast<uintptr_t>(mips) % 16 != 0)
+    return fail(g, TWS_ERR_INVALID, "terrain_rgba and mips must be 16-byte aligned");
+  if (reinterpret_cast<uintptr_t>(flowmap) % 4 != 0)
+    return fail(g, TWS_ERR_INVALID, "flowmap_rg16f must be 4-byte aligned");
   int w = g->W, h = g->H;
   for (int l = 1; l <= mip_levels; ++l) {
     if (w < 2 || h < 2) return fail(g, TWS_ERR_INVALID, "mip level smaller than 1x1");

@@ -71,6 +71,111 @@ __global__ void surface_kernel(const float* __restrict__ b, const float* __restr
   }
 }
 
+// The same per-texel arithmetic, four cells per thread for widths that are a
+// multiple of 4: 16-byte loads and stores (the packed outputs' rows then start
+// on 16-byte boundaries, and so do the pitched inputs' rows).
+__global__ void surface_kernel4(const float* __restrict__ b, const float* __restrict__ d,
+                                const float2* __restrict__ v, int W, int H, int pitch,
+                                tws_surface_out o) {
+  const int x = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= W || y >= H) return;
+  const size_t i = (size_t)y * pitch + x;
+  const size_t out = (size_t)y * W + x;
+  const float4 b4 = *reinterpret_cast<const float4*>(b + i);
+  const float4 d4 = *reinterpret_cast<const float4*>(d + i);
+  const float dc[4] = {d4.x, d4.y, d4.z, d4.w};
+  const float h[4] = {fadd(d4.x, b4.x), fadd(d4.y, b4.y), fadd(d4.z, b4.z), fadd(d4.w, b4.w)};
+  if (o.height) *reinterpret_cast<float4*>(o.height + out) = make_float4(h[0], h[1], h[2], h[3]);
+  if (o.dry)
+    *reinterpret_cast<uchar4*>(o.dry + out) =
+        make_uchar4(dc[0] < 0.1f, dc[1] < 0.1f, dc[2] < 0.1f, dc[3] < 0.1f);
+  if (o.render_height) {
+    float t[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      t[k] = fsub(h[k], 0.1f);
+      if (dc[k] < 0.1f) t[k] = fsub(t[k], 10.0f);
+    }
+    *reinterpret_cast<float4*>(o.render_height + out) = make_float4(t[0], t[1], t[2], t[3]);
+  }
+  if (o.normal) {
+    const int ym = y == 0 ? H - 1 : y - 1, yp = y + 1 == H ? 0 : y + 1;
+    const int xm = x == 0 ? W - 1 : x - 1, xp = x + 4 == W ? 0 : x + 4;
+    const size_t iu = (size_t)ym * pitch + x, id = (size_t)yp * pitch + x;
+    const float4 bu = *reinterpret_cast<const float4*>(b + iu);
+    const float4 du = *reinterpret_cast<const float4*>(d + iu);
+    const float4 bd = *reinterpret_cast<const float4*>(b + id);
+    const float4 dd = *reinterpret_cast<const float4*>(d + id);
+    const float hu[4] = {fadd(du.x, bu.x), fadd(du.y, bu.y), fadd(du.z, bu.z), fadd(du.w, bu.w)};
+    const float hd[4] = {fadd(dd.x, bd.x), fadd(dd.y, bd.y), fadd(dd.z, bd.z), fadd(dd.w, bd.w)};
+    const float hl = surf(b, d, (size_t)y * pitch + xm), hr = surf(b, d, (size_t)y * pitch + xp);
+    float n[12];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float h2 = k < 3 ? h[k + 1] : hr, h3 = k > 0 ? h[k - 1] : hl;
+      const float A = fsub(hd[k], hu[k]), B = fsub(h2, h3);
+      const float nx = -B, ny = 1.0f, nz = -A;
+      const float len = __fsqrt_rn(fadd(fadd(fmul(nx, nx), fmul(ny, ny)), fmul(nz, nz)));
+      n[3 * k + 0] = fdiv(nx, len);
+      n[3 * k + 1] = fdiv(ny, len);
+      n[3 * k + 2] = fdiv(nz, len);
+    }
+    float4* no = reinterpret_cast<float4*>(o.normal + 3 * out);
+    no[0] = make_float4(n[0], n[1], n[2], n[3]);
+    no[1] = make_float4(n[4], n[5], n[6], n[7]);
+    no[2] = make_float4(n[8], n[9], n[10], n[11]);
+  }
+  if (o.flow_speed || o.foam) {
+    const float4 v01 = *reinterpret_cast<const float4*>(v + i);
+    const float4 v23 = *reinterpret_cast<const float4*>(v + i + 2);
+    const float vx[4] = {v01.x, v01.z, v23.x, v23.z}, vy[4] = {v01.y, v01.w, v23.y, v23.w};
+    float sp[4], fo[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float fx = half_round(vx[k]), fy = half_round(vy[k]);
+      const float s2 = fadd(fmul(fx, fx), fmul(fy, fy));
+      sp[k] = __fsqrt_rn(s2);
+      fo[k] = saturate01(fmul(s2, 0.00004f));
+    }
+    if (o.flow_speed)
+      *reinterpret_cast<float4*>(o.flow_speed + out) = make_float4(sp[0], sp[1], sp[2], sp[3]);
+    if (o.foam) *reinterpret_cast<float4*>(o.foam + out) = make_float4(fo[0], fo[1], fo[2], fo[3]);
+  }
+}
+
+// TerrainData (RGBA32F) and the RG16F flow map in one pass, four cells per
+// thread, for widths that are a multiple of 4 (either output may be null).
+__global__ void export_kernel4(const float* __restrict__ b, const float* __restrict__ d,
+                               const float2* __restrict__ v, int W, int H, int pitch,
+                               float4* __restrict__ rgba, __half2* __restrict__ flowmap) {
+  const int x = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= W || y >= H) return;
+  const size_t i = (size_t)y * pitch + x;
+  const size_t out = (size_t)y * W + x;
+  if (rgba) {
+    const float4 b4 = *reinterpret_cast<const float4*>(b + i);
+    const float4 d4 = *reinterpret_cast<const float4*>(d + i);
+    rgba[out + 0] = make_float4(b4.x, 0.3f, 0.3f, d4.x);
+    rgba[out + 1] = make_float4(b4.y, 0.3f, 0.3f, d4.y);
+    rgba[out + 2] = make_float4(b4.z, 0.3f, 0.3f, d4.z);
+    rgba[out + 3] = make_float4(b4.w, 0.3f, 0.3f, d4.w);
+  }
+  if (flowmap) {
+    const float4 v01 = *reinterpret_cast<const float4*>(v + i);
+    const float4 v23 = *reinterpret_cast<const float4*>(v + i + 2);
+    const __half2 h0 = __floats2half2_rn(v01.x, v01.y), h1 = __floats2half2_rn(v01.z, v01.w);
+    const __half2 h2 = __floats2half2_rn(v23.x, v23.y), h3 = __floats2half2_rn(v23.z, v23.w);
+    uint4 packed;
+    packed.x = *reinterpret_cast<const uint32_t*>(&h0);
+    packed.y = *reinterpret_cast<const uint32_t*>(&h1);
+    packed.z = *reinterpret_cast<const uint32_t*>(&h2);
+    packed.w = *reinterpret_cast<const uint32_t*>(&h3);
+    *reinterpret_cast<uint4*>(flowmap + out) = packed;
+  }
+}
+
 __global__ void terrain_rgba_kernel(const float* __restrict__ b, const float* __restrict__ d,
                                     int W, int H, int pitch, float4* __restrict__ out) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -109,9 +214,22 @@ dim3 grid2d(int w, int h) { return dim3((w + 31) / 32, (h + 7) / 8); }
 
 }  // namespace
 
+// The four-cell kernels need W % 4 == 0 and every caller-owned output on a
+// 16-byte boundary (the dry mask on a 4-byte one); the library's own inputs
+// always are (256-byte aligned buffers, pitch a multiple of 32).
+static bool aligned(const void* p, uintptr_t a) {
+  return (reinterpret_cast<uintptr_t>(p) & (a - 1)) == 0;
+}
+
 cudaError_t launch_surface(const float* b, const float* d, const float2* v, int W, int H,
                            int pitch, const tws_surface_out& o, cudaStream_t s) {
-  surface_kernel<<<grid2d(W, H), dim3(32, 8), 0, s>>>(b, d, v, W, H, pitch, o);
+  const bool wide = W % 4 == 0 && aligned(o.height, 16) && aligned(o.render_height, 16) &&
+                    aligned(o.normal, 16) && aligned(o.flow_speed, 16) && aligned(o.foam, 16) &&
+                    aligned(o.dry, 4);
+  if (wide)
+    surface_kernel4<<<grid2d(W / 4, H), dim3(32, 8), 0, s>>>(b, d, v, W, H, pitch, o);
+  else
+    surface_kernel<<<grid2d(W, H), dim3(32, 8), 0, s>>>(b, d, v, W, H, pitch, o);
   count_launch();
   return cudaGetLastError();
 }
@@ -119,15 +237,25 @@ cudaError_t launch_surface(const float* b, const float* d, const float2* v, int 
 cudaError_t launch_export(const float* b, const float* d, const float2* v, int W, int H,
                           int pitch, float* terrain_rgba, uint16_t* flowmap, int mip_levels,
                           float* mips, cudaStream_t s) {
-  if (flowmap) {
-    flowmap_kernel<<<grid2d(W, H), dim3(32, 8), 0, s>>>(v, W, H, pitch,
-                                                         reinterpret_cast<__half2*>(flowmap));
+  const bool wide = W % 4 == 0 && aligned(terrain_rgba, 16) && aligned(flowmap, 16);
+  if (wide && (flowmap || terrain_rgba)) {
+    export_kernel4<<<grid2d(W / 4, H), dim3(32, 8), 0, s>>>(
+        b, d, v, W, H, pitch, reinterpret_cast<float4*>(terrain_rgba),
+        reinterpret_cast<__half2*>(flowmap));
     count_launch();
+  } else {
+    if (flowmap) {
+      flowmap_kernel<<<grid2d(W, H), dim3(32, 8), 0, s>>>(v, W, H, pitch,
+                                                           reinterpret_cast<__half2*>(flowmap));
+      count_launch();
+    }
+    if (terrain_rgba) {
+      terrain_rgba_kernel<<<grid2d(W, H), dim3(32, 8), 0, s>>>(
+          b, d, W, H, pitch, reinterpret_cast<float4*>(terrain_rgba));
+      count_launch();
+    }
   }
   if (terrain_rgba) {
-    terrain_rgba_kernel<<<grid2d(W, H), dim3(32, 8), 0, s>>>(b, d, W, H, pitch,
-                                                              reinterpret_cast<float4*>(terrain_rgba));
-    count_launch();
     const float4* src = reinterpret_cast<const float4*>(terrain_rgba);
     float4* dst = reinterpret_cast<float4*>(mips);
     int sw = W, sh = H;

@@ -19,7 +19,7 @@ def tws():
     return t
 
 
-@pytest.mark.parametrize("W,H", [(96, 80), (33, 257), (1, 5)])
+@pytest.mark.parametrize("W,H", [(96, 80), (260, 130), (33, 257), (1, 5)])
 def test_surface_outputs_match_oracle(tws, oracle, W, H):
     import torch
     p = tws.params_physical(boundary=tws.BOUNDARY_OPEN)
@@ -47,7 +47,7 @@ def test_surface_outputs_match_oracle(tws, oracle, W, H):
         assert got["dry"].any() and (got["flow_speed"] > 0).any()
 
 
-@pytest.mark.parametrize("W,H,levels", [(64, 48, 3), (100, 37, 2), (256, 256, 8)])
+@pytest.mark.parametrize("W,H,levels", [(64, 48, 3), (100, 37, 2), (38, 21, 2), (256, 256, 8)])
 def test_texture_export_matches_oracle(tws, oracle, W, H, levels):
     import torch
     with tws.Grid(W, H) as g:
@@ -77,3 +77,38 @@ def test_texture_export_matches_oracle(tws, oracle, W, H, levels):
     for lvl, m in enumerate(want_mips, 1):
         assert_bitexact(got_mips[off:off + m.size].reshape(m.shape), m, f"mip {lvl}")
         off += m.size
+
+
+def test_unaligned_outputs(tws, oracle):
+    """Surface outputs 4 bytes past a 16-byte boundary are written one cell at
+    a time (the four-cell kernels need aligned rows), with the same values; so
+    is a 4-byte aligned flow map.  RGBA32F buffers that are not 16-byte
+    aligned are refused before any launch."""
+    import torch
+    W, H = 96, 40
+    with tws.Grid(W, H) as g:
+        g.generate_scene(5, 40.0, 15.0)
+        g.set_sources(tws.rain_disks(5, W, H, 6, 0.05, 1))
+        g.step(11)
+        d, _, v = g.download(flux=False)
+        b = g.download_terrain()
+        raw = torch.zeros(W * H + 4, dtype=torch.float32, device="cuda")
+        height = raw[1:1 + W * H]  # 4 bytes past an aligned start
+        fm_raw = torch.zeros(2 * W * H + 2, dtype=torch.int16, device="cuda")
+        flowmap = fm_raw[2:2 + 2 * W * H]  # 4 bytes past an aligned start
+        rgba_raw = torch.zeros(W * H * 4 + 4, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        g.surface(tws.SurfaceOut(height.data_ptr(), None, None, None, None, None))
+        g.export_textures(None, flowmap.data_ptr(), 0, None)
+        with pytest.raises(tws.TwsError) as e:
+            g.export_textures(rgba_raw.data_ptr() + 4, None, 0, None)
+        assert e.value.code == tws.ERR_INVALID
+        with pytest.raises(tws.TwsError) as e:
+            g.surface(tws.SurfaceOut(raw.data_ptr() + 2, None, None, None, None, None))
+        assert e.value.code == tws.ERR_INVALID
+        g.sync()
+        got_h = height.cpu().numpy().reshape(H, W)
+        got_fm = flowmap.cpu().numpy().reshape(H, W, 2)
+    want = oracle.surface(b, d, v)
+    assert_bitexact(got_h, want["height"], "height")
+    assert np.array_equal(got_fm.view(np.uint16), v.astype(np.float16).view(np.uint16))

@@ -79,3 +79,8 @@ def test_noalloc_rejects_grids_beyond_its_scratch(tws):
     assert b"TWS_VOLUME_NOALLOC_MAX_ROWS" in tws.lib().tws_error_string(rc)
     assert tws.lib().tws_volume_noalloc(None, 8, 8, 32, 1.0, dummy, None) == tws.ERR_INVALID
     assert tws.lib().tws_volume_noalloc(dummy, 64, 8, 32, 1.0, dummy, None) == tws.ERR_INVALID
+    # misaligned depth (floats) or result (a double): refused before any launch
+    assert tws.lib().tws_volume_noalloc(C.c_void_p(258), 8, 8, 32, 1.0, dummy,
+                                        None) == tws.ERR_INVALID
+    assert tws.lib().tws_volume_noalloc(dummy, 8, 8, 32, 1.0, C.c_void_p(260),
+                                        None) == tws.ERR_INVALID

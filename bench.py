@@ -415,11 +415,12 @@ def run_ours(args):
 #   surface: read b, d, v (16); write height, render height, flow speed, foam
 #            (4 each), normal (12), dry mask (1)
 #   export:  flow map (read v 8, write 2 halves 4) + TerrainData RGBA32F (read b, d 8,
-#            write 16); its mip pyramid adds, per level l >= 1, the read of level
-#            l - 1 and the write of level l: 16 (4/3 + 1/3) bytes per cell in all
+#            write 16); its mip pyramid adds the write of every level l >= 1,
+#            16 / 4^l bytes per cell each: 16/3 in all (the reads of the
+#            intermediate levels that build the next are not counted)
 SURFACE_BYTES_PER_CELL = 45.0
 EXPORT_BYTES_PER_CELL = 36.0
-MIPS_BYTES_PER_CELL = 16.0 * (4.0 / 3.0 + 1.0 / 3.0)
+MIPS_BYTES_PER_CELL = 16.0 / 3.0
 
 
 def renderer_leg(tws, torch, g, stream, size, peak):

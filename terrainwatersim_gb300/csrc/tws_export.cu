@@ -176,6 +176,55 @@ __global__ void export_kernel4(const float* __restrict__ b, const float* __restr
   }
 }
 
+__device__ __forceinline__ float avg4(float a, float b, float c, float d);
+
+// export_kernel4's work for a 4 x 2 block of cells, plus the two texels of
+// the first mip level those cells make (W % 4 == 0, H even): the level is
+// built from registers instead of re-reading TerrainData.
+__global__ void export_mip1_kernel4(const float* __restrict__ b, const float* __restrict__ d,
+                                    const float2* __restrict__ v, int W, int H, int pitch,
+                                    float4* __restrict__ rgba, __half2* __restrict__ flowmap,
+                                    float4* __restrict__ mip1) {
+  const int x = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+  const int y = 2 * (blockIdx.y * blockDim.y + threadIdx.y);
+  if (x >= W || y >= H) return;
+  float4 t[2][4];
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const size_t i = (size_t)(y + r) * pitch + x;
+    const size_t out = (size_t)(y + r) * W + x;
+    const float4 b4 = *reinterpret_cast<const float4*>(b + i);
+    const float4 d4 = *reinterpret_cast<const float4*>(d + i);
+    t[r][0] = make_float4(b4.x, 0.3f, 0.3f, d4.x);
+    t[r][1] = make_float4(b4.y, 0.3f, 0.3f, d4.y);
+    t[r][2] = make_float4(b4.z, 0.3f, 0.3f, d4.z);
+    t[r][3] = make_float4(b4.w, 0.3f, 0.3f, d4.w);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) rgba[out + k] = t[r][k];
+    if (flowmap) {
+      const float4 v01 = *reinterpret_cast<const float4*>(v + i);
+      const float4 v23 = *reinterpret_cast<const float4*>(v + i + 2);
+      const __half2 h0 = __floats2half2_rn(v01.x, v01.y), h1 = __floats2half2_rn(v01.z, v01.w);
+      const __half2 h2 = __floats2half2_rn(v23.x, v23.y), h3 = __floats2half2_rn(v23.z, v23.w);
+      uint4 packed;
+      packed.x = *reinterpret_cast<const uint32_t*>(&h0);
+      packed.y = *reinterpret_cast<const uint32_t*>(&h1);
+      packed.z = *reinterpret_cast<const uint32_t*>(&h2);
+      packed.w = *reinterpret_cast<const uint32_t*>(&h3);
+      *reinterpret_cast<uint4*>(flowmap + out) = packed;
+    }
+  }
+  // level 1 texel (x/2 + j, y/2) from cells (x + 2j, y), (x + 2j + 1, y),
+  // (x + 2j, y + 1), (x + 2j + 1, y + 1), in mip_kernel's order
+  const size_t m = (size_t)(y / 2) * (W / 2) + x / 2;
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    const float4 a = t[0][2 * j], c0 = t[0][2 * j + 1], c = t[1][2 * j], e = t[1][2 * j + 1];
+    mip1[m + j] = make_float4(avg4(a.x, c0.x, c.x, e.x), avg4(a.y, c0.y, c.y, e.y),
+                              avg4(a.z, c0.z, c.z, e.z), avg4(a.w, c0.w, c.w, e.w));
+  }
+}
+
 __global__ void terrain_rgba_kernel(const float* __restrict__ b, const float* __restrict__ d,
                                     int W, int H, int pitch, float4* __restrict__ out) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -238,7 +287,14 @@ cudaError_t launch_export(const float* b, const float* d, const float2* v, int W
                           int pitch, float* terrain_rgba, uint16_t* flowmap, int mip_levels,
                           float* mips, cudaStream_t s) {
   const bool wide = W % 4 == 0 && aligned(terrain_rgba, 16) && aligned(flowmap, 16);
-  if (wide && (flowmap || terrain_rgba)) {
+  // with mips, the first level comes out of the same pass (even heights)
+  const bool fuse_mip1 = wide && terrain_rgba && mips && mip_levels >= 1 && H % 2 == 0;
+  if (fuse_mip1) {
+    export_mip1_kernel4<<<grid2d(W / 4, H / 2), dim3(32, 8), 0, s>>>(
+        b, d, v, W, H, pitch, reinterpret_cast<float4*>(terrain_rgba),
+        reinterpret_cast<__half2*>(flowmap), reinterpret_cast<float4*>(mips));
+    count_launch();
+  } else if (wide && (flowmap || terrain_rgba)) {
     export_kernel4<<<grid2d(W / 4, H), dim3(32, 8), 0, s>>>(
         b, d, v, W, H, pitch, reinterpret_cast<float4*>(terrain_rgba),
         reinterpret_cast<__half2*>(flowmap));
@@ -258,8 +314,15 @@ cudaError_t launch_export(const float* b, const float* d, const float2* v, int W
   if (terrain_rgba) {
     const float4* src = reinterpret_cast<const float4*>(terrain_rgba);
     float4* dst = reinterpret_cast<float4*>(mips);
-    int sw = W, sh = H;
-    for (int l = 1; l <= mip_levels && mips; ++l) {
+    int sw = W, sh = H, l = 1;
+    if (fuse_mip1) {  // level 1 is written; continue from it
+      src = dst;
+      dst += (size_t)(W / 2) * (H / 2);
+      sw = W / 2;
+      sh = H / 2;
+      l = 2;
+    }
+    for (; l <= mip_levels && mips; ++l) {
       const int dw = sw / 2 > 0 ? sw / 2 : 1, dh = sh / 2 > 0 ? sh / 2 : 1;
       if (sw < 2 || sh < 2) break;
       mip_kernel<<<grid2d(dw, dh), dim3(32, 8), 0, s>>>(src, sw, dst, dw, dh);

@@ -300,3 +300,56 @@ def ref_noise():
                                                     C.c_void_p, C.c_void_p]
             _ref_noise = R
     return _ref_noise
+
+
+# --------------------------------------------------------------------------- reference render shaders
+
+_REF_RENDER_PATH = os.path.join(HERE, "_ref", "libtws_ref_render.so")
+_ref_render = None
+
+
+def ref_render_available() -> bool:
+    return os.path.exists(_REF_RENDER_PATH)
+
+
+def ref_render():
+    """The parts of the reference's water-rendering shaders that read the
+    simulation's textures (waterRender.vert, .eval's main(), .frag's
+    ComputeHeightmapNormal and flow-speed lines), built by `make -C oracle
+    ref` (see ref_glsl/render_emu.h)."""
+    global _ref_render
+    with _lock:
+        if _ref_render is None:
+            R = C.CDLL(_REF_RENDER_PATH)
+            R.tws_ref_water_vert.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+            R.tws_ref_water_eval.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+            R.tws_ref_water_frag.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                             C.c_void_p, C.c_void_p]
+            _ref_render = R
+    return _ref_render
+
+
+def ref_surface(b, d, flowmap_f16):
+    """The reference's own shader code on a square grid's state: b, d (N, N)
+    float32 and the RG16F flow map as (N, N, 2) uint16.  Returns the same keys
+    as surface()."""
+    H, W = b.shape
+    assert H == W, "the fragment shader's texel size is one number: square grids"
+    R = ref_render()
+    rgba = np.empty((H, W, 4), np.float32)
+    rgba[..., 0] = b
+    rgba[..., 1] = 0.3
+    rgba[..., 2] = 0.3
+    rgba[..., 3] = d
+    fm = np.ascontiguousarray(flowmap_f16, dtype=np.uint16)
+    height = np.empty((H, W), np.float32)
+    under = np.empty((H, W), np.int32)
+    render = np.empty((H, W), np.float32)
+    normal = np.empty((H, W, 3), np.float32)
+    speed = np.empty((H, W), np.float32)
+    foam = np.empty((H, W), np.float32)
+    R.tws_ref_water_vert(_fp(rgba), W, H, _fp(height), _fp(under))
+    R.tws_ref_water_eval(_fp(rgba), W, H, _fp(render))
+    R.tws_ref_water_frag(_fp(rgba), _fp(fm), W, _fp(normal), _fp(speed), _fp(foam))
+    return {"height": height, "render_height": render, "normal": normal, "flow_speed": speed,
+            "foam": foam, "dry": under.astype(np.uint8)}

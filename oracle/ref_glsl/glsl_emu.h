@@ -23,6 +23,7 @@
 // Build with -ffp-contract=off so that no multiply-add is fused.
 
 #pragma once
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 
@@ -85,7 +86,48 @@ struct glsl_swz2 {
     v[B] = o.y;
     return *this;
   }
+  // swizzle = swizzle writes only the two named components
+  glsl_swz2& operator=(const glsl_swz2& o) { return *this = vec2(o.v[A], o.v[B]); }
+  operator vec2() const { return vec2(v[A], v[B]); }
 };
+
+inline vec2 operator+(vec2 a, vec2 b) { return vec2(a.x + b.x, a.y + b.y); }
+inline vec2 operator*(float s, vec2 a) { return vec2(s * a.x, s * a.y); }
+inline vec2 operator*(vec2 a, float s) { return vec2(a.x * s, a.y * s); }
+inline vec2 operator+(float s, vec2 a) { return vec2(s + a.x, s + a.y); }
+
+// vec3 with the .xz / .xy swizzles the water shaders assign through.
+struct vec3 {
+  union {
+    struct {
+      float x, y, z;
+    };
+    glsl_swz2<0, 2> xz;
+    glsl_swz2<0, 1> xy;
+  };
+  vec3() { x = y = z = 0.0f; }
+  vec3(float a0, float a1, float a2) {
+    x = a0;
+    y = a1;
+    z = a2;
+  }
+  vec3(const vec3& o) { std::memcpy(this, &o, sizeof(vec3)); }
+  vec3& operator=(const vec3& o) {
+    std::memcpy(this, &o, sizeof(vec3));
+    return *this;
+  }
+};
+inline vec3 operator/(const vec3& v, float s) { return vec3(v.x / s, v.y / s, v.z / s); }
+inline float dot(const vec3& a, const vec3& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+// GLSL 4.30 section 8.5: cross(x, y) = (x1 y2 - y1 x2, x2 y0 - y2 x0, x0 y1 - y0 x1)
+inline vec3 cross(const vec3& a, const vec3& b) {
+  return vec3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
+}
+inline float sqrt(float v) { return std::sqrt(v); }
+// normalize and length are implementation-defined in precision (GLSL 4.30
+// section 4.7.1); this emulation takes v / sqrt(dot(v, v)), correctly rounded
+// at each operation.
+inline vec3 normalize(const vec3& v) { return v / sqrt(dot(v, v)); }
 
 struct vec4 {
   union {
@@ -96,8 +138,15 @@ struct vec4 {
       float r, g, b, a;
     };
     glsl_swz2<2, 3> zw;
+    glsl_swz2<0, 1> xy;
   };
   vec4() { x = y = z = w = 0.0f; }
+  vec4(const vec3& v, float a3) {
+    x = v.x;
+    y = v.y;
+    z = v.z;
+    w = a3;
+  }
   explicit vec4(float s) { x = y = z = w = s; }
   vec4(float a0, float a1, float a2, float a3) {
     x = a0;
@@ -110,6 +159,8 @@ struct vec4 {
     std::memcpy(this, &o, sizeof(vec4));
     return *this;
   }
+  float& operator[](int i) { return (&x)[i]; }
+  float operator[](int i) const { return (&x)[i]; }
   vec4& operator*=(float s) {
     x = x * s;
     y = y * s;

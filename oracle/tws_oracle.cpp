@@ -454,7 +454,11 @@ void tws_oracle_surface(int W, int H, const float* b, const float* d, const floa
         const int xm = x == 0 ? W - 1 : x - 1, xp = x + 1 == W ? 0 : x + 1;
         const int ym = y == 0 ? H - 1 : y - 1, yp = y + 1 == H ? 0 : y + 1;
         const float A = h(x, yp) - h(x, ym), B = h(xp, y) - h(xm, y);
-        const float nx = -B, ny = 1.0f, nz = -A;
+        // GLSL's cross(x, y) = (x1 y2 - y1 x2, x2 y0 - y2 x0, x0 y1 - y0 x1)
+        // on x = (0, A, 1), y = (1, B, 0), product by product (the zero
+        // products keep the sign of zero of a flat surface)
+        const float nx = A * 0.0f - B * 1.0f, ny = 1.0f * 1.0f - 0.0f * 0.0f,
+                    nz = 0.0f * B - 1.0f * A;
         const float len = std::sqrt((nx * nx + ny * ny) + nz * nz);
         normal[3 * i + 0] = nx / len;
         normal[3 * i + 1] = ny / len;

@@ -30,6 +30,18 @@ __device__ __forceinline__ float surf(const float* b, const float* d, size_t i) 
 
 __device__ __forceinline__ float half_round(float v) { return __half2float(__float2half_rn(v)); }
 
+// cross((0, A, 1), (1, B, 0)) evaluated component by component as GLSL
+// defines cross(x, y) = (x1 y2 - y1 x2, x2 y0 - y2 x0, x0 y1 - y0 x1)
+// (waterRender.frag:63-65): (A*0 - B*1, 1*1 - 0*0, 0*B - 1*A) = (A*0 - B, 1,
+// 0*B - A).  The products with zero keep the sign of zero a flat surface
+// gives (A = 0 or B = 0), which -B and -A alone would flip.
+__device__ __forceinline__ void heightmap_cross(float A, float B, float& nx, float& ny,
+                                                float& nz) {
+  nx = fsub(fmul(A, 0.0f), B);
+  ny = 1.0f;
+  nz = fsub(fmul(0.0f, B), A);
+}
+
 __global__ void surface_kernel(const float* __restrict__ b, const float* __restrict__ d,
                                const float2* __restrict__ v, int W, int H, int pitch,
                                tws_surface_out o) {
@@ -55,8 +67,8 @@ __global__ void surface_kernel(const float* __restrict__ b, const float* __restr
     const float h2 = surf(b, d, (size_t)y * pitch + xp);
     const float h3 = surf(b, d, (size_t)y * pitch + xm);
     const float A = fsub(h1, h0), B = fsub(h2, h3);
-    // cross((0, A, 1), (1, B, 0)) = (-B, 1, -A)
-    const float nx = -B, ny = 1.0f, nz = -A;
+    float nx, ny, nz;
+    heightmap_cross(A, B, nx, ny, nz);
     const float len = __fsqrt_rn(fadd(fadd(fmul(nx, nx), fmul(ny, ny)), fmul(nz, nz)));
     o.normal[3 * out + 0] = fdiv(nx, len);
     o.normal[3 * out + 1] = fdiv(ny, len);
@@ -115,7 +127,8 @@ __global__ void surface_kernel4(const float* __restrict__ b, const float* __rest
     for (int k = 0; k < 4; ++k) {
       const float h2 = k < 3 ? h[k + 1] : hr, h3 = k > 0 ? h[k - 1] : hl;
       const float A = fsub(hd[k], hu[k]), B = fsub(h2, h3);
-      const float nx = -B, ny = 1.0f, nz = -A;
+      float nx, ny, nz;
+      heightmap_cross(A, B, nx, ny, nz);
       const float len = __fsqrt_rn(fadd(fadd(fmul(nx, nx), fmul(ny, ny)), fmul(nz, nz)));
       n[3 * k + 0] = fdiv(nx, len);
       n[3 * k + 1] = fdiv(ny, len);

@@ -10,7 +10,7 @@ can pin the oracle and the CUDA kernels without the reference checkout.
 The reference's native border is the open sink (out-of-range image loads read
 zero), so the fixtures use TWS_BOUNDARY_OPEN.
 
-Run:  python tests/golden/make_golden.py    (needs the reference checkout)
+Run:  TWS_REFERENCE_ROOT=<reference checkout> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -55,6 +55,9 @@ def case_bumps_48x32():
 
 def main():
     O.build(ref=True)
+    if "--render-only" in sys.argv:
+        write_render_case()
+        return
     if not O.ref_available():
         raise SystemExit("reference library not built (no reference checkout?)")
     for case in (case_brush_64(), case_bumps_48x32()):
@@ -68,6 +71,43 @@ def main():
                             flowmap_f16=fm)
         print(f"wrote {path}: volume {O.volume(d_out):.6f}")
     write_reference_scene()
+    write_render_case()
+
+
+RENDER_CASE = dict(N=64, seed=12, fill=15.0, brush=(25.6, 19.2, 40.0, 6.0), steps=25)
+
+
+def render_case_state():
+    """The state the render fixture is taken on: the benchmark terrain (seed
+    12) on 64 x 64 cells, open border, one brush stroke, 25 steps of the
+    benchmark's physical parameters -- water flowing, some cells dry."""
+    c = RENDER_CASE
+    N = c["N"]
+    b, d = O.terrain(c["seed"], N, N, 40.0, c["fill"])
+    f = np.zeros((N, N, 4), np.float32)
+    v = np.zeros((N, N, 2), np.float32)
+    kf, ka, cc = O.params_physical()
+    bx, by, size_sq, intensity = c["brush"]
+    O.sources_f32(d, [(O.SOURCE_BRUSH, bx, by, size_sq, intensity)])
+    O.step_f32(b, d, f, v, kf, ka, cc, O.BOUNDARY_OPEN, nsteps=c["steps"])
+    return b, d, v
+
+
+def write_render_case():
+    """What the reference's water-rendering shaders compute from that state
+    (their own code, compiled by `make -C oracle ref`; see
+    oracle/ref_glsl/render_emu.h): surface and tessellated heights, the dry
+    flag, the heightmap normal, the flow speed and the foam blend factor."""
+    if not O.ref_render_available():
+        raise SystemExit("reference render library not built")
+    b, d, v = render_case_state()
+    fm = v.astype(np.float16).view(np.uint16)
+    r = O.ref_surface(b, d, fm)
+    path = os.path.join(HERE, "ref_render_64.npz")
+    np.savez_compressed(path, b=b, d=d, v=v, flowmap_f16=fm,
+                        **{"out_" + k: val for k, val in r.items()},
+                        **{"case_" + k: np.array(val) for k, val in RENDER_CASE.items()})
+    print(f"wrote {path}")
 
 
 def write_reference_scene():

@@ -7,7 +7,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import assert_bitexact
+from conftest import assert_bitexact, load_golden
 
 pytestmark = pytest.mark.gpu
 
@@ -45,6 +45,39 @@ def test_surface_outputs_match_oracle(tws, oracle, W, H):
     assert np.array_equal(got["dry"], want["dry"])
     if W > 1:  # (a 1-wide open grid has drained by now)
         assert got["dry"].any() and (got["flow_speed"] > 0).any()
+
+
+def test_surface_matches_reference_render_fixture(tws):
+    """tws_surface against the reference's own water-rendering shader code
+    (tests/golden/ref_render_64.npz, made by running waterRender.vert, the
+    main() of waterRender.eval and waterRender.frag's ComputeHeightmapNormal
+    and flow-speed lines on the CPU): the same state on the GPU, then every
+    output bit for bit."""
+    import torch
+    g0 = load_golden("ref_render_64")
+    N = int(g0["case_N"])
+    bx, by, size_sq, intensity = g0["case_brush"].tolist()
+    p = tws.params_physical(boundary=tws.BOUNDARY_OPEN)
+    with tws.Grid(N, N, p) as g:
+        g.generate_scene(int(g0["case_seed"]), 40.0, float(g0["case_fill"]))
+        g.apply_source((tws.SOURCE_BRUSH, bx, by, size_sq, intensity))
+        g.step(int(g0["case_steps"]))
+        d, _, v = g.download(flux=False)
+        assert_bitexact(d, g0["d"], "depth")
+        assert_bitexact(v, g0["v"], "flow map")
+        bufs = {k: torch.zeros((N, N), dtype=torch.float32, device="cuda")
+                for k in ("height", "render_height", "flow_speed", "foam")}
+        bufs["normal"] = torch.zeros((N, N, 3), dtype=torch.float32, device="cuda")
+        bufs["dry"] = torch.zeros((N, N), dtype=torch.uint8, device="cuda")
+        torch.cuda.synchronize()
+        out = tws.SurfaceOut(*[bufs[k].data_ptr() for k in
+                               ("height", "render_height", "normal", "flow_speed", "foam", "dry")])
+        g.surface(out)
+        g.sync()
+        got = {k: t.cpu().numpy() for k, t in bufs.items()}
+    for k in ("height", "render_height", "normal", "flow_speed", "foam"):
+        assert_bitexact(got[k], g0["out_" + k], k)
+    assert np.array_equal(got["dry"], g0["out_dry"])
 
 
 @pytest.mark.parametrize("W,H,levels", [(64, 48, 3), (100, 37, 2), (38, 21, 2), (256, 256, 8)])

@@ -251,3 +251,46 @@ def test_reference_noise_scene_live(oracle, N, gen, seed):
     b, d = oracle.reference_terrain(N, N, 300.0, seed, gen)
     assert_bitexact(b, rb, "terrain")
     assert_bitexact(d, rd, "depth")
+
+
+# ---------------------------------------------------------------- the renderer's reads, pinned
+
+RENDER_KEYS = ("height", "render_height", "normal", "flow_speed", "foam")
+
+
+def test_oracle_surface_matches_reference_render_golden(oracle):
+    """The oracle's renderer-side arithmetic against the reference's own
+    water-rendering shader code (waterRender.vert, .eval main(), .frag
+    ComputeHeightmapNormal and flow speed), run on the CPU by make_golden.py."""
+    import sys
+    sys.path.insert(0, str(__import__("pathlib").Path(__file__).parent / "golden"))
+    import make_golden
+
+    g = load_golden("ref_render_64")
+    b, d, v = make_golden.render_case_state()
+    assert_bitexact(b, g["b"], "terrain")
+    assert_bitexact(d, g["d"], "depth")
+    assert_bitexact(v, g["v"], "flow map (float)")
+    assert g["out_dry"].any() and (g["out_flow_speed"] > 0).any()  # the case exercises both
+    got = oracle.surface(g["b"], g["d"], g["v"])
+    for k in RENDER_KEYS:
+        assert_bitexact(got[k], g["out_" + k], k)
+    assert np.array_equal(got["dry"], g["out_dry"])
+
+
+@pytest.mark.parametrize("N,seed", [(32, 5), (64, 6), (128, 7)])
+def test_oracle_surface_matches_reference_render_live(oracle, N, seed):
+    if not oracle.ref_render_available():
+        pytest.skip("reference render shaders not built here (no reference checkout)")
+    rng = np.random.default_rng(seed)
+    b = rng.uniform(0.0, 10.0, (N, N)).astype(np.float32)
+    d = np.maximum(0.0, rng.uniform(-1.0, 2.0, (N, N))).astype(np.float32)
+    d[: N // 4] = 0.0
+    b[: N // 8] = 3.0  # flat dry rows: zero slopes, whose signs the normal keeps
+    v = rng.uniform(-40.0, 40.0, (N, N, 2)).astype(np.float32)
+    want = oracle.ref_surface(b, d, v.astype(np.float16).view(np.uint16))
+    got = oracle.surface(b, d, v)
+    for k in RENDER_KEYS:
+        assert not np.isnan(want[k]).any(), k  # every sample was a texel centre
+        assert_bitexact(got[k], want[k], k)
+    assert np.array_equal(got["dry"], want["dry"])

@@ -24,7 +24,9 @@ def test_surface_matches_numpy(oracle):
     assert np.array_equal(got["dry"], (d < f32(0.1)).astype(np.uint8))
     A = (np.roll(h, -1, axis=0) - np.roll(h, 1, axis=0)).astype(np.float32)  # h(y+1) - h(y-1)
     B = (np.roll(h, -1, axis=1) - np.roll(h, 1, axis=1)).astype(np.float32)  # h(x+1) - h(x-1)
-    nx, ny, nz = -B, np.ones_like(B), -A
+    # GLSL cross((0, A, 1), (1, B, 0)) product by product: (A*0 - B, 1, 0*B - A)
+    zero = np.float32(0.0)
+    nx, ny, nz = (A * zero - B).astype(np.float32), np.ones_like(B), (zero * B - A).astype(np.float32)
     ln = np.sqrt(((nx * nx + ny * ny) + nz * nz).astype(np.float32)).astype(np.float32)
     n = np.stack([nx / ln, ny / ln, nz / ln], axis=-1).astype(np.float32)
     assert_bitexact(got["normal"], n, "normal")

@@ -196,12 +196,9 @@ TWS_API int tws_set_variant(tws_grid* grid, int variant);
  * default, about two seconds), sets the grid's error word and returns
  * without writing that tile.  The next tws_sync then reports TWS_ERR_TIMEOUT
  * once and clears the word; the state is undefined after it and must be
- * uploaded again, and the context stays usable.
- * tws_test_inject_missing_bytes makes every tile load declare `bytes` more
- * (a multiple of 16, 0..4096) than it moves, so that each wait runs out:
- * the test hook for that path.  0 turns it off. */
+ * uploaded again, and the context stays usable.  (The test hook that makes
+ * the waits run out is declared in tws_testing.h, not here.) */
 TWS_API int tws_set_wait_limit(tws_grid* grid, long long sm_cycles);
-TWS_API int tws_test_inject_missing_bytes(tws_grid* grid, int bytes);
 
 /* Autotuner: times every variant for `trial_steps` steps on this grid's
  * current state (restored afterwards, so the simulation is unchanged), picks
@@ -262,8 +259,11 @@ TWS_API int tws_volume(tws_grid* grid, double* out);
  * (128 KB) inside libtws.so, which every GPU that loads the library holds
  * until the process exits.  Grids taller than that return
  * TWS_ERR_TOO_LARGE.  The first call on each device looks up that array's
- * device address once (cudaGetSymbolAddress); make the first call before any
- * stream capture.  All calls share the array and it keeps the last call's
+ * device address once (cudaGetSymbolAddress) and keeps it for the life of
+ * the process; make the first call before any stream capture.  A
+ * cudaDeviceReset (or anything else that recreates the device's primary
+ * context) after that first call is not supported: the kept address would
+ * be stale.  All calls share the array and it keeps the last call's
  * partial sums (every partial is rewritten, nothing needs clearing), so two
  * calls that can run on the GPU at the same time -- on different streams,
  * or from different host threads -- race and may return wrong sums:
@@ -300,7 +300,11 @@ TWS_API int tws_surface(tws_grid* grid, const tws_surface_out* out);
  * `mips` (level l is floor(W/2^l) x floor(H/2^l) RGBA32F texels; every level
  * must be at least 1 x 1).  Any pointer may be NULL (mips need terrain_rgba).
  * terrain_rgba and mips must be 16-byte aligned and flowmap_rg16f 4-byte
- * aligned (TWS_ERR_INVALID otherwise).  Asynchronous on the grid's stream. */
+ * aligned (TWS_ERR_INVALID otherwise).  The fast path (four cells per thread,
+ * the first mip level written from registers) also needs flowmap_rg16f on a
+ * 16-byte boundary and a width that is a multiple of 4; otherwise the call
+ * runs one cell per thread, with the same results.  Asynchronous on the
+ * grid's stream. */
 TWS_API int tws_export_textures(tws_grid* grid, float* terrain_rgba, uint16_t* flowmap_rg16f,
                                 int mip_levels, float* mips);
 

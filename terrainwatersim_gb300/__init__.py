@@ -111,7 +111,7 @@ def _declare(L):
         "tws_variant_info": ([i, vp, vp, vp, vp, vp], i),
         "tws_set_variant": ([vp, i], i),
         "tws_set_wait_limit": ([vp, C.c_longlong], i),
-        "tws_test_inject_missing_bytes": ([vp, i], i),
+        "tws_test_drop_tile_loads": ([vp, i], i),
         "tws_autotune": ([vp, i, vp], i),
         "tws_resident_fits": ([i, i, i], i),
         "tws_set_resident": ([vp, i], i),
@@ -368,10 +368,11 @@ class Grid:
         (0: the default)."""
         _check(lib().tws_set_wait_limit(self._h, sm_cycles), self._h)
 
-    def test_inject_missing_bytes(self, nbytes: int):
-        """Test hook: every tile load declares `nbytes` more than it moves,
-        so its bounded wait runs out (0 turns it off)."""
-        _check(lib().tws_test_inject_missing_bytes(self._h, nbytes), self._h)
+    def test_drop_tile_loads(self, drop: bool = True):
+        """Test hook (tws_testing.h): every tile load arms its barrier but
+        issues no copy, so its bounded wait runs out with nothing in flight
+        (False turns it off)."""
+        _check(lib().tws_test_drop_tile_loads(self._h, 1 if drop else 0), self._h)
 
     def set_resident(self, on: bool = True, ctas: int | None = None):
         """Run the steps with the resident kernel (the whole grid in one

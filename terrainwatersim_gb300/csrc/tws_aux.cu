@@ -498,9 +498,20 @@ extern "C" TWS_API int tws_volume_noalloc(const float* depth, int width, int hei
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   // One block per row: block r writes partial r (every partial is rewritten,
   // so nothing needs clearing); one block then adds the partials in row order.
-  tws::volume_rows_kernel<<<height, tws::kVolThreads, 0, st>>>(depth, width, height, pitch,
-                                                               scratch);
-  tws::volume_final_kernel<<<1, tws::kVolThreads, 0, st>>>(scratch, height, cell_area, out);
-  tws::count_launch(2);
-  return cudaGetLastError() == cudaSuccess ? TWS_OK : TWS_ERR_CUDA;
+  // Each launch's own result is checked (cudaLaunchKernelEx returns it), so
+  // an earlier error pending on this thread is neither reported nor cleared.
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3((unsigned)height);
+  cfg.blockDim = dim3(tws::kVolThreads);
+  cfg.stream = st;
+  cudaError_t e = cudaLaunchKernelEx(&cfg, tws::volume_rows_kernel, depth, width, height, pitch,
+                                     scratch);
+  if (e == cudaSuccess) {
+    tws::count_launch(1);
+    cfg.gridDim = dim3(1);
+    e = cudaLaunchKernelEx(&cfg, tws::volume_final_kernel, static_cast<const double*>(scratch),
+                           height, cell_area, out);
+    if (e == cudaSuccess) tws::count_launch(1);
+  }
+  return e == cudaSuccess ? TWS_OK : TWS_ERR_CUDA;
 }

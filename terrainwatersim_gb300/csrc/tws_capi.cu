@@ -60,7 +60,7 @@ struct tws_grid {
   int err_host[1] = {0};
   CUtensorMap* desc = nullptr;  // device copies of the maps, 5 per variant (batched kernel)
   long long wait_cycles = kDefaultWaitCycles;  // SM clocks a tile-load wait may take
-  int missing_tx = 0;     // test hook: bytes each tile load declares but never moves
+  int drop_loads = 0;     // test hook: tile loads arm their barrier but issue no copy
   tws_batch* batch = nullptr;  // batch this grid belongs to (its stream is the batch's)
   cudaStream_t home_stream = nullptr;
   // Asynchronous host I/O, made on first use: packed staging (upload b, d, f
@@ -228,7 +228,7 @@ StepArgs make_step_args(const tws_grid* g) {
   a.flux_inv_scale = 1.0f / g->flux_scale;
   a.err = g->err;
   a.wait_cycles = g->wait_cycles;
-  a.missing_tx = g->missing_tx;
+  a.drop_loads = g->drop_loads;
   return a;
 }
 
@@ -606,11 +606,9 @@ TWS_API int tws_set_wait_limit(tws_grid* g, long long sm_cycles) {
   return TWS_OK;
 }
 
-TWS_API int tws_test_inject_missing_bytes(tws_grid* g, int bytes) {
-  // a multiple of 16 keeps the declared count a legal transaction size
-  if (!g || bytes < 0 || bytes > 4096 || bytes % 16 != 0)
-    return fail(g, TWS_ERR_INVALID, "missing bytes must be a multiple of 16 in 0..4096");
-  g->missing_tx = bytes;
+TWS_API int tws_test_drop_tile_loads(tws_grid* g, int drop) {
+  if (!g || (drop != 0 && drop != 1)) return fail(g, TWS_ERR_INVALID, "drop must be 0 or 1");
+  g->drop_loads = drop;
   return TWS_OK;
 }
 

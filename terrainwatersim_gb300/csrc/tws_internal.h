@@ -9,6 +9,7 @@
 #include <string>
 
 #include "../../include/tws.h"
+#include "../../include/tws_testing.h"
 
 namespace tws {
 
@@ -35,7 +36,7 @@ struct StepArgs {
   float flux_inv_scale;  // F16 storage: f = stored * flux_inv_scale
   int* err;              // device error word (bounded-wait time-outs)
   long long wait_cycles; // bounded waits give up after this many SM clocks
-  int missing_tx;        // test hook: bytes a tile load declares beyond what it moves
+  int drop_loads;        // test hook: tile loads arm their barrier but issue no copy
 };
 
 // Kernel variants (temporal block depth K x tile).

@@ -113,8 +113,16 @@ __device__ __forceinline__ unsigned char* align_smem(unsigned char* raw) {
 
 // Bounded wait on phase `parity`: gives up after `limit` SM clocks (by default
 // about two seconds; a tile load takes microseconds).  On time-out: record
-// the error, wait once more (bounded) so no copy is left writing into shared
-// memory, report false.
+// the error, wait once more (bounded) for the barrier, report false.
+//
+// What the second wait can and cannot ensure: a copy that lands late but
+// lands completes the barrier, so the CTA leaves only after it.  A copy that
+// never completes cannot be observed or cancelled from the SM; the CTA then
+// leaves after the second limit with that copy still pending.  Only a fault
+// of the memory system can cause that, and the grid's error word reports the
+// time-out either way, after which the host reloads the state.  The test
+// hook (tws_test_drop_tile_loads) arms the barrier without issuing any copy,
+// so the tested path has nothing in flight.
 __device__ bool wait_bounded(uint64_t* bar, uint32_t parity, int* err, long long limit) {
   if (mbar_try_wait(bar, parity)) return true;
   const long long t0 = clock64();
@@ -179,14 +187,16 @@ struct Tile {
 };
 
 // The three TMA loads of the tile at (x0, y0) into one stage buffer.
-// `missing` (normally 0) is the test hook of tws_test_inject_missing_bytes:
-// the barrier then expects bytes that never arrive and its wait runs out.
+// `drop` (normally 0) is the test hook of tws_test_drop_tile_loads: the
+// barrier is armed for the tile's bytes but no copy is issued, so its wait
+// runs out with nothing in flight.
 template <class T, bool F16>
 __device__ __forceinline__ void issue_tile(unsigned char* st, uint64_t* bar,
                                            const CUtensorMap* tm_b, const CUtensorMap* tm_d,
                                            const CUtensorMap* tm_f, int x0, int y0,
-                                           int missing = 0) {
-  mbar_expect_tx(bar, T::TX_BYTES + (uint32_t)missing);
+                                           int drop = 0) {
+  mbar_expect_tx(bar, T::TX_BYTES);
+  if (drop) return;
   tma_load_2d(st + T::ST_B, tm_b, x0 - T::HX, y0 - T::HY, bar);
   tma_load_2d(st + T::ST_D, tm_d, x0 - T::HX, y0 - T::HY, bar);
   if (F16) {
@@ -642,7 +652,7 @@ __global__ void __launch_bounds__(kThreads)
         int tx0, ty0;
         tile_origin(t, tx0, ty0);
         issue_tile<T, F16>(smem + s * T::ST_BYTES, &bars[s], &tm_b, &tm_d, &tm_f, tx0, ty0,
-                           a.missing_tx);
+                           a.drop_loads);
       }
     }
   }
@@ -670,7 +680,19 @@ __global__ void __launch_bounds__(kThreads)
     }
 
     const bool ok = wait_bounded(&bars[s], parity, a.err, a.wait_cycles);
-    if (__syncthreads_or(!ok)) return;  // every thread leaves together on a time-out
+    if (__syncthreads_or(!ok)) {  // every thread leaves together on a time-out
+      if (STAGES > 1 && tid == 0) {
+        // the loads already issued into the other stages are waited for
+        // (bounded) first, so that none is left writing into shared memory
+#pragma unroll
+        for (int j = 1; j < STAGES; ++j) {
+          if (t + j * stride < num_tiles)
+            wait_bounded(&bars[(it + j) % STAGES], (uint32_t)(((it + j) / STAGES) & 1), a.err,
+                         a.wait_cycles);
+        }
+      }
+      return;
+    }
 
     const bool interior =
         x0 - T::HX >= 0 && y0 - T::HY >= 0 && x0 + TX + T::HX <= a.W && y0 + TY + T::HY <= a.H;
@@ -696,7 +718,7 @@ __global__ void __launch_bounds__(kThreads)
         int nx0, ny0;
         tile_origin(tn, nx0, ny0);
         fence_proxy_async_smem();
-        issue_tile<T, F16>(st, &bars[s], &tm_b, &tm_d, &tm_f, nx0, ny0, a.missing_tx);
+        issue_tile<T, F16>(st, &bars[s], &tm_b, &tm_d, &tm_f, nx0, ny0, a.drop_loads);
       }
     }
   }
@@ -755,7 +777,7 @@ __global__ void __launch_bounds__(kThreads, MINB)
       tensormap_acquire(tm + 1 + p);
       tensormap_acquire(tm + 3 + p);
     }
-    issue_tile<T, F16>(smem, bar, tm, tm + 1 + p, tm + 3 + p, x0, y0, a.missing_tx);
+    issue_tile<T, F16>(smem, bar, tm, tm + 1 + p, tm + 3 + p, x0, y0, a.drop_loads);
   }
   uint32_t mask = 0;
 #pragma unroll

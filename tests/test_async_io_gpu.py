@@ -205,7 +205,7 @@ def test_timeout_during_pipelined_io_is_reported_and_recovers(tws, oracle):
     with tws.Grid(W, H, p) as g:
         g.set_steps_per_launch(2)
         g.set_wait_limit(2_000_000)
-        g.test_inject_missing_bytes(16)
+        g.test_drop_tile_loads(True)
         g.upload_async(b, d, f)
         g.step(4)
         g.download_async(out)
@@ -214,7 +214,7 @@ def test_timeout_during_pipelined_io_is_reported_and_recovers(tws, oracle):
             g.sync()
         assert e.value.code == tws.ERR_TIMEOUT
         g.sync()  # reported once
-        g.test_inject_missing_bytes(0)
+        g.test_drop_tile_loads(False)
         g.upload_async(b, d, f)
         g.step(6)
         g.download_async(out)

@@ -1,6 +1,6 @@
-"""Failure detection on the GPU without a fault: every tile load is made to
-declare bytes that never arrive, so each kernel's bounded barrier wait runs
-out.  The kernel records the time-out in the grid's error word and returns;
+"""Failure detection on the GPU without a fault: every tile load arms its
+barrier but issues no copy (tws_test_drop_tile_loads, include/tws_testing.h),
+so each kernel's bounded barrier wait runs out with nothing in flight.  The kernel records the time-out in the grid's error word and returns;
 tws_sync reports TWS_ERR_TIMEOUT once, and the same grid and context then
 run a normal step that matches the oracle bit for bit."""
 from __future__ import annotations
@@ -53,7 +53,7 @@ def test_lost_tile_load_times_out_and_grid_recovers(tws, oracle, pick):
         g.set_variant(variant)
         g.upload(b, d, f)
         g.set_wait_limit(WAIT_LIMIT)
-        g.test_inject_missing_bytes(16)
+        g.test_drop_tile_loads(True)
         g.step(2)
         with pytest.raises(tws.TwsError) as e:
             g.sync()
@@ -61,7 +61,7 @@ def test_lost_tile_load_times_out_and_grid_recovers(tws, oracle, pick):
         # reported once: the word is clear again
         g.sync()
         # the context and grid stay usable: reload and run normally
-        g.test_inject_missing_bytes(0)
+        g.test_drop_tile_loads(False)
         g.set_wait_limit(0)
         g.upload(b, d, f)
         g.step(6)
@@ -83,7 +83,7 @@ def test_batched_lost_tile_load_times_out_and_recovers(tws, oracle):
     with tws.Batch() as batch, tws.Grid(W, H, p) as g:
         g.upload(b, d, f)
         g.set_wait_limit(WAIT_LIMIT)
-        g.test_inject_missing_bytes(32)
+        g.test_drop_tile_loads(True)
         batch.add(g)
         batch.step(4)
         with pytest.raises(tws.TwsError) as e:
@@ -91,7 +91,7 @@ def test_batched_lost_tile_load_times_out_and_recovers(tws, oracle):
         assert e.value.code == tws.ERR_TIMEOUT
         batch.sync()
         batch.remove(g)
-        g.test_inject_missing_bytes(0)
+        g.test_drop_tile_loads(False)
         g.set_wait_limit(0)
         g.upload(b, d, f)
         batch.add(g)
@@ -108,8 +108,7 @@ def test_batched_lost_tile_load_times_out_and_recovers(tws, oracle):
 
 def test_hook_arguments_checked(tws):
     with tws.Grid(16, 16) as g:
-        for bad in (-16, 8, 4097 * 16):
-            with pytest.raises(tws.TwsError):
-                g.test_inject_missing_bytes(bad)
+        for bad in (-1, 2, 16):
+            assert tws.lib().tws_test_drop_tile_loads(g._h, bad) == tws.ERR_INVALID
         with pytest.raises(tws.TwsError):
             g.set_wait_limit(-1)

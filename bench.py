@@ -21,6 +21,13 @@ Printed JSON line (rank 0):
                  compared with the GPU's for the same steps (full grid)
   plain/blocked  the plain kernel (1 step per launch) and the temporally
                  blocked kernel, both timed
+  batched_vs_plain  64 uneven grids (2000 steps) in one batched launch per
+                 step against the plain kernel one grid at a time, with FP64
+                 checks on 4 sampled grids
+  serving        the serving loop on the first --serving-requests requests of
+                 the seeded Poisson stream: time-to-completion p50/p95/p99 and
+                 aggregate rate against serial plain-kernel execution, at 70%
+                 load and saturated
 --impl reference times the CPU port of the reference's path on the host cores
 (the reference itself is an OpenGL program that cannot run on this machine).
 """
@@ -68,6 +75,13 @@ def parse():
                          "batched; c4: 16384^2 FP16 flux; c5: serving loop")
     ap.add_argument("--requests", type=int, default=2000, help="c5: requests in the stream")
     ap.add_argument("--max-steps", type=int, default=20000, help="c5: largest step count")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the batched-vs-plain leg (the 64-grid configuration)")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving leg")
+    ap.add_argument("--c4-window-steps", type=int, default=1600,
+                    help="c4: steps before the 1024^2 window is compared with the FP64 oracle")
+    ap.add_argument("--serving-requests", type=int, default=300,
+                    help="serving leg of the default run: the first N requests of the stream")
     return ap.parse_args()
 
 
@@ -274,8 +288,21 @@ def run_ours(args):
     value = aggregate_gcell_steps(cells, chain * steps, ws, total)
     launch_s = total / max(1, launches)  # only step kernels run in the timed region
     cell_steps_per_launch = cells * best_k
-    achieved = bpc * cell_steps_per_launch / launch_s / 1e9
+    # Compulsory HBM bytes of one launch: the state is read once and written
+    # once whatever the launch's temporal depth K (52 B per cell for FP32
+    # flux, 36 B for FP16).  The K-scaled "effective" rate is reported beside it.
+    compulsory = bpc * cells
+    achieved = compulsory / launch_s / 1e9
+    effective = bpc * cell_steps_per_launch / launch_s / 1e9
     tpc = ncu_traffic_per_cell(best_k, args.flux)
+    plain = variants.get(0)
+    if plain is None:  # no sweep: time the plain kernel alone for its top-level keys
+        g.generate_scene(2026, 40.0, 15.0)
+        t, _, n = time_device(tws, torch, g, stream, 0, chain, max(3, steps // 5), warmup, dist)
+        plain = dict(seconds=max_over_ranks(dist, t), launches=n, steps=max(3, steps // 5))
+    plain_launch_s = plain["seconds"] / max(1, plain["launches"])
+    plain_value = cells * chain * plain["steps"] * ws / plain["seconds"] / 1e9
+    plain_gbs = bpc * cells / plain_launch_s / 1e9
 
     # end to end through the C ABI with pinned host buffers
     hb = torch.empty((size, size), dtype=torch.float32, pin_memory=True).numpy()
@@ -359,8 +386,15 @@ def run_ours(args):
             },
             "hbm_frac_of_measured": round(achieved / peak, 4),
             "hbm_frac_of_8tbs_nominal": round(achieved / 8000.0, 4),
+            "plain_gcell_steps_per_s": round(plain_value, 3),
+            "plain_hbm_gbs": round(plain_gbs, 1),
+            "plain_hbm_frac_of_measured": round(plain_gbs / peak, 4),
+            "plain_kernel": "step_kernel<K=1,32x32> (variant 0): one step per launch, "
+                            f"{bpc:.0f} B per cell-step compulsory",
             "p50_ms": round(per_sorted[len(per) // 2], 4),
             "p99_ms": round(per_sorted[min(len(per) - 1, int(0.99 * len(per)))], 4),
+            "p50_p99_note": "per bench step (a chain of simulation steps) on the resident grid; "
+                            "request time-to-completion percentiles are under 'serving'",
             "roofline": {
                 "bound": "hbm",
                 "achieved": round(achieved, 1),
@@ -368,7 +402,14 @@ def run_ours(args):
                 "unit": "GB/s",
                 "frac": round(achieved / peak, 4),
                 "peak_kind": peak_kind,
-                "algorithmic_bytes_per_launch": bpc * cell_steps_per_launch,
+                "algorithmic_bytes_per_launch": compulsory,
+                "algorithmic_bytes_note": f"{bpc:.0f} B per cell x {cells} cells: the state read "
+                                          f"and written once per launch (K = {best_k} steps "
+                                          "per launch)",
+                "effective_gbs": round(effective, 1),
+                "effective_note": f"{bpc:.0f} B per cell-step x K cell-steps per cell per "
+                                  "launch / launch time (an un-blocked kernel's traffic for the "
+                                  "same work, not bytes moved)",
                 "launch_us": round(launch_s * 1e6, 2),
                 "traffic": round(tpc * cells, 0) if tpc else None,
                 "dram_gbs": round(tpc * cells / launch_s / 1e9, 1) if tpc else None,
@@ -405,6 +446,24 @@ def run_ours(args):
         if ws == 1 and not args.no_cpu:
             result["cpu_baseline"] = cpu_baseline_leg(tws, g, size, args.cpu_seconds)
     g.close()
+    if rank == 0 and ws == 1:
+        # the metric's comparisons, measured in the same run: many grids batched
+        # against the plain kernel one grid at a time, and the serving loop's
+        # time-to-completion percentiles against serial plain execution
+        if not args.no_batched:
+            torch.cuda.empty_cache()
+            result["batched_vs_plain"] = run_c3(args)
+            result["batched_vs_plain_ratio"] = result["batched_vs_plain"][
+                "speedup_vs_one_grid_at_a_time"]
+        if not args.no_serving:
+            torch.cuda.empty_cache()
+            sv = serving_leg(args.serving_requests, args.max_steps, C5_ARMS_DEFAULT)
+            result["serving"] = sv
+            arm = sv.get("served_fp16_batched", {})
+            result["serving_latency_s"] = {k: arm.get("latency_s_" + k)
+                                           for k in ("p50", "p95", "p99")}
+            result["serving_vs_serial_plain"] = {"at_70pct_load": sv.get("aggregate_speedup"),
+                                                 "saturated": sv.get("saturated_speedup")}
     if dist is not None:
         dist.barrier()
         dist.destroy_process_group()
@@ -877,11 +936,39 @@ def run_c4(args):
                      "rel_volume_drift_vs_fp64_bookkeeping": abs(vol - exact) / exact}
         g.close()
         torch.cuda.empty_cache()
-    # depth error on a 1024^2 window: GPU (full grid) vs FP64 oracle (crop)
-    short, win = 200, 1024
+    # Depth error on a 1024^2 window centred on the first rain disk, where the
+    # water moves (the initial state d = max(0, 15 - b) is a lake at rest, so a
+    # window away from every disk would see no flow at all).  The FP64 oracle
+    # runs on a crop that holds the window's whole domain of dependence (two
+    # cells per step); where the crop reaches the grid's edge it is the grid's
+    # own closed wall.
+    short, win = args.c4_window_steps, 1024
     margin = 2 * short + 8
-    x0 = y0 = N // 2 - win // 2
-    cx0, cy0, cw = x0 - margin, y0 - margin, win + 2 * margin
+    cx, cy = int(rain[0][1]), int(rain[0][2])
+    x0 = min(max(0, cx - win // 2), N - win)
+    y0 = min(max(0, cy - win // 2), N - win)
+    cx0, cy0 = max(0, x0 - margin), max(0, y0 - margin)
+    cx1, cy1 = min(N, x0 + win + margin), min(N, y0 + win + margin)
+    b, d0 = O.terrain(2026, N, N, 40.0, 15.0)
+    b64 = np.ascontiguousarray(b[cy0:cy1, cx0:cx1]).astype(np.float64)
+    d64 = np.ascontiguousarray(d0[cy0:cy1, cx0:cx1]).astype(np.float64)
+    d0w = d0[y0:y0 + win, x0:x0 + win].astype(np.float64)
+    del b, d0
+    f64 = np.zeros(b64.shape + (4,), np.float64)
+    srcs = [(O.SOURCE_DISK, s[1] - cx0, s[2] - cy0, s[3], 0.01) for s in rain]
+    t0 = time.perf_counter()
+    O.step_f64(b64, d64, f64, None, *O.params_physical(), O.BOUNDARY_CLOSED, srcs, nsteps=short)
+    t64 = time.perf_counter() - t0
+    ref = d64[y0 - cy0:y0 - cy0 + win, x0 - cx0:x0 - cx0 + win].copy()
+    del b64, d64, f64
+    moved = np.abs(ref - d0w) > 1e-3
+    out["window"] = {"origin": [x0, y0], "size": win, "steps": short,
+                     "centre_rain_disk": [cx, cy, int(rain[0][3])],
+                     "fp64_crop": [cx1 - cx0, cy1 - cy0],
+                     "fp64_seconds": round(t64, 1),
+                     "cells_moved_over_1mm_frac": round(float(moved.mean()), 4),
+                     "max_depth_change_m": float(np.abs(ref - d0w).max())}
+    wins = {}
     for name, fs in (("fp16_flux", tws.FLUX_F16), ("fp32", tws.FLUX_F32)):
         g = tws.Grid(N, N, p, fs)
         g.set_sources(rain)
@@ -889,20 +976,18 @@ def run_c4(args):
         g.step(short)
         d, _, _ = g.download(flux=False, velocity=False)
         g.close()
-        b, d0 = O.terrain(2026, N, N, 40.0, 15.0)
-        b64 = np.ascontiguousarray(b[cy0:cy0 + cw, cx0:cx0 + cw]).astype(np.float64)
-        d64 = np.ascontiguousarray(d0[cy0:cy0 + cw, cx0:cx0 + cw]).astype(np.float64)
-        del b, d0
-        f64 = np.zeros((cw, cw, 4), np.float64)
-        srcs = [(O.SOURCE_DISK, s[1] - cx0, s[2] - cy0, s[3], 0.01) for s in rain]
-        O.step_f64(b64, d64, f64, None, *O.params_physical(), O.BOUNDARY_CLOSED, srcs,
-                   nsteps=short)
-        ref = d64[margin:margin + win, margin:margin + win]
-        gw = d[y0:y0 + win, x0:x0 + win]
+        gw = d[y0:y0 + win, x0:x0 + win].astype(np.float64)
+        del d
+        wins[name] = gw
+        err = np.abs(gw - ref)
         out[name]["window_steps"] = short
-        out[name]["window_max_abs_depth_err_vs_fp64"] = float(np.abs(gw - ref).max())
-        out[name]["window_rel_max_depth_err_vs_fp64"] = float(np.abs(gw - ref).max()
+        out[name]["window_max_abs_depth_err_vs_fp64"] = float(err.max())
+        out[name]["window_rel_max_depth_err_vs_fp64"] = float(err.max()
                                                                / max(1e-30, np.abs(ref).max()))
+        out[name]["window_mean_abs_depth_err_vs_fp64"] = float(err.mean())
+        out[name]["window_rel_volume_diff_vs_fp64"] = float(abs(gw.sum() - ref.sum()) / ref.sum())
+    out["window"]["fp16_vs_fp32_max_abs_depth_diff"] = float(
+        np.abs(wins["fp16_flux"] - wins["fp32"]).max())
     return out
 
 
@@ -922,15 +1007,29 @@ def c5_workload(n, max_steps, seed=2026):
     return out
 
 
-def run_c5(args):
-    """Serving loop vs serial plain-kernel execution of the same request stream."""
+C5_ARMS_ALL = (("served_fp16_batched", "f16", False, True),
+               ("served_fp32_batched", "f32", False, True),
+               ("serial_fp32_plain", "f32", True, True),
+               ("saturated_served_fp16_batched", "f16", False, False),
+               ("saturated_served_fp32_batched", "f32", False, False),
+               ("saturated_serial_fp32_plain", "f32", True, False))
+# the default bench line's serving leg: the served FP16 path against serial
+# plain-kernel execution, at 70% load (latency) and saturated (capacity)
+C5_ARMS_DEFAULT = tuple(a for a in C5_ARMS_ALL if "fp32_batched" not in a[0])
+
+
+def serving_leg(n, max_steps, arms=C5_ARMS_ALL):
+    """Serving loop vs serial plain-kernel execution of the same request
+    stream (the first n requests of the seeded stream).  Each arm reports
+    time-to-completion percentiles over its requests, aggregate Gcell-steps/s
+    over the makespan, and each request's final volume against exact FP64
+    bookkeeping (initial FP64 volume plus the rain added)."""
     import torch
 
     import terrainwatersim_gb300 as tws
     from terrainwatersim_gb300 import serve
 
-    n = args.requests
-    work = c5_workload(n, args.max_steps)
+    work = c5_workload(n, max_steps)
     total_cell_steps = float(sum(w["W"] * w["H"] * w["steps"] for w in work))
     p = tws.params_physical(0.02, 9.81, 1.0, 1.0, 0.998, tws.BOUNDARY_CLOSED)
 
@@ -970,18 +1069,13 @@ def run_c5(args):
                                      float(arrivals[i]))
 
     out = {"config": f"{n} Poisson requests, side log-uniform 64-4096, aspect 1-2, steps "
-                     f"log-uniform 100-{args.max_steps}, one rain disk each, closed walls, "
+                     f"log-uniform 100-{max_steps}, one rain disk each, closed walls, "
                      f"arrival rate for {int(load * 100)}% load of the measured FP16 capacity",
            "requests": n, "total_cell_steps": total_cell_steps,
            "capacity_gcell_steps_per_s": round(capacity / 1e9, 3),
            "arrival_rate_per_s": round(rate, 3), "arrival_span_s": round(float(arrivals[-1]), 3)}
-    runs = (("served_fp16_batched", tws.FLUX_F16, False, True),
-            ("served_fp32_batched", tws.FLUX_F32, False, True),
-            ("serial_fp32_plain", tws.FLUX_F32, True, True),
-            ("saturated_served_fp16_batched", tws.FLUX_F16, False, False),
-            ("saturated_served_fp32_batched", tws.FLUX_F32, False, False),
-            ("saturated_serial_fp32_plain", tws.FLUX_F32, True, False))
-    for name, fs, serial, poisson in runs:
+    for name, fs_name, serial, poisson in arms:
+        fs = tws.FLUX_F16 if fs_name == "f16" else tws.FLUX_F32
         with serve.Server(memory_budget_bytes=120e9, flux_storage=fs) as srv:
             for r in requests():
                 if not poisson:  # every request present at the start: capacity
@@ -1007,15 +1101,24 @@ def run_c5(args):
             "chains": st["chains"],
             "max_rel_volume_drift_vs_fp64_bookkeeping": float(max(drift)),
         }
-    out["aggregate_speedup"] = round(out["served_fp16_batched"]["aggregate_gcell_steps_per_s"]
-                                     / out["serial_fp32_plain"]["aggregate_gcell_steps_per_s"], 3)
-    out["saturated_speedup"] = round(
-        out["saturated_served_fp16_batched"]["aggregate_gcell_steps_per_s"]
-        / out["saturated_serial_fp32_plain"]["aggregate_gcell_steps_per_s"], 3)
-    out["saturated_speedup_fp32_served"] = round(
-        out["saturated_served_fp32_batched"]["aggregate_gcell_steps_per_s"]
-        / out["saturated_serial_fp32_plain"]["aggregate_gcell_steps_per_s"], 3)
+
+    def ratio(a, b):
+        if a in out and b in out:
+            return round(out[a]["aggregate_gcell_steps_per_s"]
+                         / out[b]["aggregate_gcell_steps_per_s"], 3)
+        return None
+    out["aggregate_speedup"] = ratio("served_fp16_batched", "serial_fp32_plain")
+    out["saturated_speedup"] = ratio("saturated_served_fp16_batched",
+                                     "saturated_serial_fp32_plain")
+    sp = ratio("saturated_served_fp32_batched", "saturated_serial_fp32_plain")
+    if sp is not None:
+        out["saturated_speedup_fp32_served"] = sp
     return out
+
+
+def run_c5(args):
+    """Serving loop vs serial plain-kernel execution of the full request stream."""
+    return serving_leg(args.requests, args.max_steps, C5_ARMS_ALL)
 
 
 def main():

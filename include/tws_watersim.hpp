@@ -89,14 +89,36 @@ class WaterSim {
   }
 
   /// Terrain::PerformSimulationStep (Terrain.cpp:240-277): a fixed-step
-  /// accumulator, at most 10 steps per call.  Returns the steps taken.
+  /// accumulator, at most 10 steps per call.  Returns the steps taken.  When
+  /// texture targets are set (SetTextureTargets), a call that took a step
+  /// also rewrites them, mip pyramid included, as the reference regenerates
+  /// TerrainData's mips after its steps (Terrain.cpp:272-276); without
+  /// targets the renderer reads the device buffers (GetBuffers) directly.
   unsigned PerformSimulationStep(double lastFrameSeconds) {
     m_timeSinceLastSimulationStep += lastFrameSeconds;
     unsigned n = (unsigned)(m_timeSinceLastSimulationStep / m_simulationStepLength);
     m_timeSinceLastSimulationStep -= m_simulationStepLength * n;
     if (n > 10u) n = 10u;
-    if (n > 0) check(tws_step(m_grid, (int)n), m_grid);
+    if (n > 0) {
+      check(tws_step(m_grid, (int)n), m_grid);
+      if (m_texRgba || m_texFlowmap)
+        check(tws_export_textures(m_grid, m_texRgba, m_texFlowmap, m_texMipLevels, m_texMips),
+              m_grid);
+    }
     return n;
+  }
+
+  /// Device buffers (caller-owned, layouts of tws_export_textures) that
+  /// PerformSimulationStep refreshes after every call that took a step:
+  /// TerrainData as RGBA32F, the RG16F flow map, and `mipLevels` levels of
+  /// TerrainData's mip pyramid in `mips`.  All null (the default) turns the
+  /// refresh off.
+  void SetTextureTargets(float* terrainRgba, uint16_t* flowmapRg16f, int mipLevels = 0,
+                         float* mips = nullptr) {
+    m_texRgba = terrainRgba;
+    m_texFlowmap = flowmapRg16f;
+    m_texMipLevels = mips ? mipLevels : 0;
+    m_texMips = mips;
   }
 
   /// Advance exactly n steps.
@@ -180,6 +202,11 @@ class WaterSim {
   double m_timeSinceLastSimulationStep;
   float m_heightScale = 300.0f;  // Terrain.cpp:25
   int m_noiseScenes = 0;         // noise tables drawn so far
+  // texture targets PerformSimulationStep refreshes (none by default)
+  float* m_texRgba = nullptr;
+  uint16_t* m_texFlowmap = nullptr;
+  int m_texMipLevels = 0;
+  float* m_texMips = nullptr;
 };
 
 }  // namespace tws

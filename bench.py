@@ -217,6 +217,22 @@ def aggregate_gcell_steps(cells: int, sim_steps: int, world_size: int, seconds: 
 
 # ------------------------------------------------------------------ our arm
 
+def variant_form(v):
+    """How a variant runs: one CTA per tile, persistent CTAs, register
+    streaming, or a row sweep (with its rows per loop trip)."""
+    kind = v[5] if len(v) > 5 else 0
+    if kind == 1:
+        return "stream"
+    if kind == 2:
+        return f"sweep_u{v[3]}"
+    return "persistent" if v[3] > 1 else "pertile"
+
+
+def kernel_name(v):
+    kind = v[5] if len(v) > 5 else 0
+    return {1: "stream_kernel", 2: "sweep_kernel"}.get(kind, "step_kernel")
+
+
 def scene(tws, size):
     p = tws.params_physical(0.02, 9.81, 1.0, 1.0, 0.998, tws.BOUNDARY_CLOSED)
     rain = tws.rain_disks(2026, size, size, 64, 0.01, 1)
@@ -413,11 +429,12 @@ def run_ours(args):
                 "launch_us": round(launch_s * 1e6, 2),
                 "traffic": round(tpc * cells, 0) if tpc else None,
                 "dram_gbs": round(tpc * cells / launch_s / 1e9, 1) if tpc else None,
-                "kernel": f"step_kernel<K={best_k},{vinfo[best_v][1]}x{vinfo[best_v][2]}>",
+                "kernel": f"{kernel_name(vinfo[best_v])}<K={best_k},"
+                          f"{vinfo[best_v][1]}x{vinfo[best_v][2]}>",
             },
             "variants": {
                 (f"{i}_{'plain' if vinfo[i][0] == 1 else 'blocked_k%d' % vinfo[i][0]}"
-                 f"_{vinfo[i][1]}x{vinfo[i][2]}_{'persistent' if vinfo[i][3] > 1 else 'pertile'}"): {
+                 f"_{vinfo[i][1]}x{vinfo[i][2]}_{variant_form(vinfo[i])}"): {
                     "variant": i,
                     "gcell_steps_per_s": round(cells * chain * v["steps"] * ws / v["seconds"] / 1e9,
                                                3),

@@ -185,6 +185,17 @@ TWS_API int tws_set_steps_per_launch(tws_grid* grid, int steps_per_launch);
 TWS_API int tws_variant_count(void);
 TWS_API int tws_variant_info(int variant, int* steps_per_launch, int* tile_x, int* tile_y,
                              int* stages, size_t* shared_bytes);
+/* The kind of kernel variant i, or TWS_ERR_INVALID past the last one:
+ * TWS_VARIANT_TILE (TMA-staged tiles: tile_x x tile_y output cells per CTA),
+ * TWS_VARIANT_STREAM (register streaming, one step: tile_x columns per warp
+ * walking tile_y rows) or TWS_VARIANT_SWEEP (a warp sweeps a strip of tile_x
+ * output columns down a band of tile_y rows, the steps' time levels in
+ * registers).  Only the tile variants wait on barriers that
+ * tws_set_wait_limit bounds. */
+#define TWS_VARIANT_TILE 0
+#define TWS_VARIANT_STREAM 1
+#define TWS_VARIANT_SWEEP 2
+TWS_API int tws_variant_kind(int variant);
 
 /* Pin a variant for this grid (-1: automatic -- the tuned choice for this
  * grid shape if tws_autotune ran for one, else the steps-per-launch setting). */

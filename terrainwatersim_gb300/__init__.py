@@ -109,6 +109,7 @@ def _declare(L):
         "tws_set_steps_per_launch": ([vp, i], i),
         "tws_variant_count": ([], i),
         "tws_variant_info": ([i, vp, vp, vp, vp, vp], i),
+        "tws_variant_kind": ([i], i),
         "tws_set_variant": ([vp, i], i),
         "tws_set_wait_limit": ([vp, C.c_longlong], i),
         "tws_test_drop_tile_loads": ([vp, i], i),
@@ -209,15 +210,21 @@ def rain_disks(seed: int, width: int, height: int, radius: int, rate: float, cou
     return [(s.kind, s.cx, s.cy, s.radius, s.rate) for s in arr[:count]]
 
 
+VARIANT_TILE, VARIANT_STREAM, VARIANT_SWEEP = 0, 1, 2
+
+
 def variants():
-    """[(steps_per_launch, tile_x, tile_y, stages, shared_bytes)] of the step kernel."""
+    """[(steps_per_launch, tile_x, tile_y, stages, shared_bytes, kind)] of the
+    step kernel (kind: VARIANT_TILE, VARIANT_STREAM or VARIANT_SWEEP)."""
     L = lib()
     out = []
     for i in range(L.tws_variant_count()):
         k, tx, ty, st, sm = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_size_t()
         _check(L.tws_variant_info(i, C.byref(k), C.byref(tx), C.byref(ty), C.byref(st),
                                   C.byref(sm)))
-        out.append((k.value, tx.value, ty.value, st.value, sm.value))
+        kind = L.tws_variant_kind(i)
+        _check(min(kind, 0))
+        out.append((k.value, tx.value, ty.value, st.value, sm.value, kind))
     return out
 
 

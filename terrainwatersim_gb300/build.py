@@ -21,7 +21,8 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libtws.so")
 
-SOURCES = ["tws_step.cu", "tws_stream.cu", "tws_resident.cu", "tws_aux.cu", "tws_export.cu",
+SOURCES = ["tws_step.cu", "tws_stream.cu", "tws_sweep.cu", "tws_resident.cu", "tws_aux.cu",
+           "tws_export.cu",
            "tws_capi.cu",
            "tws_serve.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -592,6 +592,15 @@ TWS_API int tws_variant_info(int i, int* k, int* tx, int* ty, int* stages, size_
   return TWS_OK;
 }
 
+TWS_API int tws_variant_kind(int i) {
+  if (i < 0 || i >= step_variant_count()) return TWS_ERR_INVALID;
+  switch (step_variant(i).kind) {
+    case kKindStream: return TWS_VARIANT_STREAM;
+    case kKindSweep: return TWS_VARIANT_SWEEP;
+    default: return TWS_VARIANT_TILE;
+  }
+}
+
 TWS_API int tws_set_variant(tws_grid* g, int variant) {
   if (!g || variant < -1 || variant >= step_variant_count())
     return fail(g, TWS_ERR_INVALID, "no such kernel variant");

@@ -44,17 +44,19 @@ struct StepVariant {
   int k;      // steps per launch
   int tx, ty; // interior tile
   int stages; // 1: one CTA per tile; 2: persistent CTAs, next tile prefetched
-  int kind;   // kKindTile (TMA-staged tiles) or kKindStream (register streaming, K = 1)
-  int ry;     // kKindStream: rows per warp strip
+  int kind;   // kKindTile (TMA-staged tiles), kKindStream (register streaming, K = 1)
+              // or kKindSweep (row sweep over column strips, K time levels in registers)
+  int ry;     // kKindStream, kKindSweep: rows per warp strip
   int hx;     // x halo of the b/d boxes (2K rounded up to 4 floats)
   int bw, bh; // b/d box
   int fw, fh; // flux box
   int sw;     // F16 staging width in cells (whole pairs)
   int uni;    // unified layout: the flux box is the b/d box
+  int ring;   // kKindSweep: rows in each lane's load ring
   size_t smem;
 };
 
-enum : int { kKindTile = 0, kKindStream = 1 };
+enum : int { kKindTile = 0, kKindStream = 1, kKindSweep = 2 };
 
 // One member grid of a batch as the batched kernel reads it from device
 // memory: its tensor maps, its step arguments and its buffers.  The maps are
@@ -111,6 +113,12 @@ int step_variant_for(int k, int flux_storage);
 cudaError_t launch_step(int variant, int flux_storage, const CUtensorMap* tm_b,
                         const CUtensorMap* tm_d, const CUtensorMap* tm_f, const float* b,
                         const float* d, const void* f, const StepArgs& a, cudaStream_t s);
+// tws_sweep.cu: K = 2..4 steps per launch, `rows` rows per warp band, a
+// ring of `ring` rows per lane (4)
+cudaError_t launch_sweep_step(int k, int rows, int ring, int flux_storage, const float* b,
+                              const float* d, const void* f, const StepArgs& a, cudaStream_t s);
+size_t sweep_smem_bytes(int flux_storage, int ring);
+int sweep_valid_columns(int k);
 // tws_stream.cu
 cudaError_t launch_stream_step(int ry, int flux_storage, const float* b, const float* d,
                                const void* f, const StepArgs& a, cudaStream_t s);

@@ -849,7 +849,7 @@ VariantEntry make_entry() {
 }
 
 struct VariantTable {
-  static constexpr int kMax = 24;
+  static constexpr int kMax = 40;
   VariantEntry e[kMax + 1];  // one spare slot: an entry past kMax is dropped, not written over n
   int n = 0;
   std::mutex mu;
@@ -882,6 +882,26 @@ struct VariantTable {
     add<4, 32, 32, 1, true>();  // 20
     add<4, 64, 16, 1, true>();  // 21
     add<3, 64, 32, 1, true>();  // 22
+    // row sweeps: 64-column warp strips, K time levels in registers
+    // (4096^2: 32-row bands beat 64- and 128-row ones, 16-row bands pay too
+    // much halo; a ring of 8 rows is no faster than 4)
+    add_sweep(2, 32, 4);   // 23
+    add_sweep(3, 32, 4);   // 24
+    add_sweep(3, 64, 4);   // 25
+    add_sweep(4, 32, 4);   // 26
+  }
+  void add_sweep(int k, int rows, int ring) {
+    VariantEntry s{};
+    s.v.k = k;
+    s.v.tx = sweep_valid_columns(k);
+    s.v.ty = rows;
+    s.v.stages = 1;
+    s.v.kind = kKindSweep;
+    s.v.ry = rows;
+    s.v.ring = ring;
+    s.v.smem = sweep_smem_bytes(TWS_FLUX_F32, ring);
+    e[n] = s;
+    if (n < kMax) ++n;
   }
   template <int K, int TX, int TY, int STAGES, bool UNI = false>
   void add() {
@@ -1007,6 +1027,8 @@ cudaError_t launch_step(int variant, int flux_storage, const CUtensorMap* tm_b,
   const int fs = flux_storage == TWS_FLUX_F16 ? TWS_FLUX_F16 : TWS_FLUX_F32;
   VariantEntry& e = t.e[variant];
   if (e.v.kind == kKindStream) return launch_stream_step(e.v.ry, fs, b, d, f, a, s);
+  if (e.v.kind == kKindSweep)
+    return launch_sweep_step(e.v.k, e.v.ry, e.v.ring, fs, b, d, f, a, s);
   if (!tm_b || !tm_d || !tm_f) return cudaErrorInvalidValue;
   const void* fn = e.fn[fs];
   const size_t smem = e.smem[fs];

@@ -1,0 +1,436 @@
+// tws_sweep.cu -- the temporally blocked step as a row sweep.
+//
+// Same arithmetic as the tiled kernels (flowUpdate.comp:34-62 then
+// flowApply.comp:32-52, K steps per launch, bit-identical to the FP32
+// transcription of the shaders), organised so that no halo is recomputed in y:
+//
+// * A warp owns a strip of 64 columns (two per lane) and sweeps it down a
+//   band of R rows.  Each lane keeps, per time level s = 0..K-1, a rolling
+//   window of the rows that level needs in registers: surface heights h of
+//   three rows, depths and terrain of two rows, new outflows of two rows.
+//   Row by row, level s computes the outflow of one row and the depth of the
+//   row above, which is the input row of level s + 1 two rows further up; the
+//   last level writes its depth, flux and flow map.  The y neighbours come
+//   from the window, the x neighbours from the lane itself or its neighbour
+//   lanes (warp shuffles).  Values of the two outermost columns of the strip
+//   go stale one more column per phase, so a strip yields 64 - 4K output
+//   columns; neighbouring strips overlap by 4K columns (their loads are L2
+//   hits).  A band also loads 2K rows above and below it, whose results are
+//   not written.
+// * The two columns of a lane are one packed f32x2 operand
+//   (add/sub/mul.rn.f32x2): each lane of it is the IEEE round-to-nearest
+//   result of its own operands.  A packed product never feeds a packed sum
+//   (the assembler would contract the pair into a fused multiply-add); those
+//   sums are scalar.
+// * Loads: each lane copies its own two cells of a row (b, d, the flux
+//   records) into a private ring of P rows in shared memory with cp.async,
+//   P - 1 rows ahead of the row it computes.  Cells off the grid are
+//   zero-filled by the copy itself (the shaders' out-of-range image loads
+//   read zero).  A lane reads back only what it copied, so no barrier is
+//   needed; cp.async.wait_group is the hardware's wait, and a slot is
+//   refilled only in the iteration after the one that read it into
+//   registers and used those values.
+//
+// HBM traffic per launch: the state once in, once out (52 B per cell for FP32
+// flux, 36 B for FP16), plus the re-read of the strip and band overlaps,
+// which L2 serves when neighbouring strips run together.
+
+#include "tws_device.cuh"
+#include "tws_internal.h"
+
+namespace tws {
+namespace {
+
+constexpr int kSweepWarps = 4;
+constexpr int kSweepThreads = 32 * kSweepWarps;
+constexpr int kSweepCols = 64;  // columns a warp loads
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+// cp.async of `bytes` (<= size) from src; the rest of the `size` bytes is zero.
+__device__ __forceinline__ void copy8(void* dst, const void* src, int bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(smem_addr(dst)), "l"(src),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void copy16(void* dst, const void* src, int bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(dst)), "l"(src),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void copy_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void copy_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// The four outflow channels (+x, -x, +y, -y) of a lane's two cells: .x of
+// each float2 is the lane's first column, .y its second.
+struct Flux2 {
+  float2 x, y, z, w;
+};
+__device__ __forceinline__ Flux2 zero_flux() {
+  const float2 z = make_float2(0.0f, 0.0f);
+  return Flux2{z, z, z, z};
+}
+
+__device__ __forceinline__ float2 max0x2(float2 v) {
+  return make_float2(max0_fast(v.x), max0_fast(v.y));
+}
+// p + q per column, with p and q packed products: scalar sums (never fadd2
+// of an fmul2 result, see the file comment)
+__device__ __forceinline__ float2 sum_products(float2 p, float2 q) {
+  return make_float2(fadd(p.x, q.x), fadd(p.y, q.y));
+}
+
+template <bool F16, int P>
+struct SweepRing {
+  // one row of a lane's ring: b and d of its two cells, then the flux records
+  // (FP32: the first cells of all lanes, then the second cells, so that a
+  // warp's 16-byte reads are conflict-free; FP16: both cells' 8 halves)
+  static constexpr int B = 0;    // 64 floats
+  static constexpr int D = 256;  // 64 floats
+  static constexpr int F = 512;  // FP32: 2 x 32 float4; FP16: 32 x 16 bytes
+  static constexpr int ROW = F + (F16 ? 512 : 1024);
+  static constexpr int WARP = ROW * P;  // P rows: P - 1 in flight
+};
+
+template <int K, bool F16, bool INTERIOR, int P>
+__device__ __forceinline__ void sweep_unit(const StepArgs& a, const float* __restrict__ gb,
+                                           const float* __restrict__ gd,
+                                           const void* __restrict__ gf, unsigned char* ring,
+                                           int xs, int y0, int R, uint32_t mask) {
+  using RG = SweepRing<F16, P>;
+  constexpr int HALO = 2 * K;
+  const int lane = threadIdx.x & 31;
+  const int W = a.W, H = a.H;
+  const size_t pitch = (size_t)a.pitch;
+  const float2 kf2 = make_float2(a.kf, a.kf), ka2 = make_float2(a.ka, a.ka);
+  const float2 cc2 = make_float2(a.c, a.c);
+  const float fscale = a.flux_scale, finv = a.flux_inv_scale;
+  const float2 fscale2 = make_float2(fscale, fscale), finv2 = make_float2(finv, finv);
+  const bool closed = a.closed != 0;
+
+  // this lane's columns
+  const int gx0 = xs + 2 * lane, gx1 = gx0 + 1;
+  const bool in0 = INTERIOR || (gx0 >= 0 && gx0 < W);
+  const bool in1 = INTERIOR || (gx1 >= 0 && gx1 < W);
+  const bool out_lane = lane >= K && lane < 32 - K;  // columns HALO .. 63 - HALO
+  const int first_row = y0 - HALO;
+  const int rows = R + 2 * HALO;  // rows loaded
+
+  // ---- the copies of row r into ring slot `slot`
+  auto issue_row = [&](int r, int slot) {
+    unsigned char* st = ring + slot * RG::ROW;
+    const bool row_in = INTERIOR || (r >= 0 && r < H);
+    const int nb = (row_in && in0) ? (in1 ? 8 : 4) : 0;
+    const size_t g = row_in ? (size_t)r * pitch + (size_t)(in0 ? gx0 : 0) : 0;
+    copy8(st + RG::B + 8 * lane, gb + g, nb);
+    copy8(st + RG::D + 8 * lane, gd + g, nb);
+    if constexpr (F16) {
+      copy16(st + RG::F + 16 * lane, reinterpret_cast<const uint2*>(gf) + g, nb * 2);
+    } else {
+      const float4* f4 = reinterpret_cast<const float4*>(gf);
+      copy16(st + RG::F + 16 * lane, f4 + g, (row_in && in0) ? 16 : 0);
+      copy16(st + RG::F + 512 + 16 * lane, f4 + g + ((row_in && in1) ? 1 : 0),
+             (row_in && in1) ? 16 : 0);
+    }
+  };
+  auto read_bd = [&](int slot, float2& b, float2& d) {
+    const unsigned char* st = ring + slot * RG::ROW;
+    b = *reinterpret_cast<const float2*>(st + RG::B + 8 * lane);
+    d = *reinterpret_cast<const float2*>(st + RG::D + 8 * lane);
+  };
+  auto read_flux = [&](int slot) -> Flux2 {
+    const unsigned char* st = ring + slot * RG::ROW;
+    if constexpr (F16) {
+      const uint4 raw = *reinterpret_cast<const uint4*>(st + RG::F + 16 * lane);
+      const float2 a0 = fmul2(__half22float2(*reinterpret_cast<const __half2*>(&raw.x)), finv2);
+      const float2 a1 = fmul2(__half22float2(*reinterpret_cast<const __half2*>(&raw.y)), finv2);
+      const float2 b0 = fmul2(__half22float2(*reinterpret_cast<const __half2*>(&raw.z)), finv2);
+      const float2 b1 = fmul2(__half22float2(*reinterpret_cast<const __half2*>(&raw.w)), finv2);
+      return Flux2{make_float2(a0.x, b0.x), make_float2(a0.y, b0.y), make_float2(a1.x, b1.x),
+                   make_float2(a1.y, b1.y)};
+    } else {
+      const float4 c0 = *reinterpret_cast<const float4*>(st + RG::F + 16 * lane);
+      const float4 c1 = *reinterpret_cast<const float4*>(st + RG::F + 512 + 16 * lane);
+      return Flux2{make_float2(c0.x, c1.x), make_float2(c0.y, c1.y), make_float2(c0.z, c1.z),
+                   make_float2(c0.w, c1.w)};
+    }
+  };
+  auto sources2 = [&](float2 dv, int r) -> float2 {
+    if (!mask || !(INTERIOR || (r >= 0 && r < H))) return dv;
+    if (in0) dv.x = add_sources(dv.x, gx0, r, a, mask);
+    if (in1) dv.y = add_sources(dv.y, gx1, r, a, mask);
+    return dv;
+  };
+
+  // ---- per-level windows (registers; every index below is a compile-time
+  // constant once the level loops are unrolled)
+  float2 H0[K], H1[K];  // h of rows ys - 1 and ys of level s's outflow row ys
+  float2 D0[K], D1[K];  // d of rows ys - 1 and ys
+  float2 B0[K], B1[K];  // terrain of rows ys - 1 and ys (it travels with the rows)
+  Flux2 N1[K], N2[K];   // new outflow of rows ys - 1 and ys - 2
+  const float2 z2 = make_float2(0.0f, 0.0f);
+#pragma unroll
+  for (int s = 0; s < K; ++s) {
+    H0[s] = H1[s] = D0[s] = D1[s] = B0[s] = B1[s] = z2;
+    N1[s] = N2[s] = zero_flux();
+  }
+
+  // the ring: rows 0 .. P - 2 in flight before the loop
+#pragma unroll
+  for (int i = 0; i < P - 1; ++i) {
+    if (i < rows) issue_row(first_row + i, i);
+    copy_commit();
+  }
+  Flux2 fin_prev = zero_flux();  // flux of the previously loaded row
+
+#pragma unroll 1
+  for (int t = 0; t < rows; ++t) {
+    const int r = first_row + t;
+    const int slot = t % P;
+    // refill the slot of row r - 1 (read in full in the previous iteration)
+    // with row r + P - 1, then wait for row r
+    if (t + P - 1 < rows) issue_row(first_row + t + P - 1, (t + P - 1) % P);
+    copy_commit();
+    copy_wait<P - 1>();
+    float2 bl, dl;
+    read_bd(slot, bl, dl);
+    const Flux2 fl = read_flux(slot);
+    // level 0's input row: the first step's sources, then h = d + b
+    float2 d_in = sources2(dl, r);
+    float2 h_in = fadd2(d_in, bl);
+    float2 b_in = bl;
+    Flux2 f_in = fin_prev;  // flux of row r - 1: level 0's outflow row
+    fin_prev = fl;
+
+#pragma unroll
+    for (int s = 0; s < K; ++s) {
+      const int ys = r - 2 * s - 1;  // this level's outflow row
+      const bool ys_in = INTERIOR || (ys >= 0 && ys < H);
+      // -- outflow of row ys, flowUpdate.comp:34-62
+      const float2 hm = H0[s], hc = H1[s], hp = h_in;
+      const float2 h_right = make_float2(hc.y, __shfl_down_sync(0xffffffffu, hc.x, 1));
+      const float2 h_left = make_float2(__shfl_up_sync(0xffffffffu, hc.y, 1), hc.x);
+      Flux2 nf;
+      {
+        const float2 e_px = fsub2(hc, h_right), e_mx = fsub2(hc, h_left);
+        const float2 e_py = fsub2(hc, hp), e_my = fsub2(hc, hm);
+        nf.x = max0x2(sum_products(fmul2(f_in.x, kf2), fmul2(e_px, ka2)));
+        nf.y = max0x2(sum_products(fmul2(f_in.y, kf2), fmul2(e_mx, ka2)));
+        nf.z = max0x2(sum_products(fmul2(f_in.z, kf2), fmul2(e_py, ka2)));
+        nf.w = max0x2(sum_products(fmul2(f_in.w, kf2), fmul2(e_my, ka2)));
+      }
+      if constexpr (!INTERIOR) {
+        if (closed) {  // no outflow across a closed wall
+          if (gx0 + 1 >= W) nf.x.x = 0.0f;
+          if (gx1 + 1 >= W) nf.x.y = 0.0f;
+          if (gx0 == 0) nf.y.x = 0.0f;
+          if (gx1 == 0) nf.y.y = 0.0f;
+          if (ys + 1 >= H) nf.z = z2;
+          if (ys == 0) nf.w = z2;
+        }
+      }
+      {
+        const float2 dc = D1[s];
+        const float2 total = fmul2(fadd2(fadd2(fadd2(nf.x, nf.y), nf.z), nf.w), cc2);
+        if (total.x > dc.x) {
+          const float sc = scale_factor(dc.x, total.x);
+          nf.x.x = fmul(nf.x.x, sc);
+          nf.y.x = fmul(nf.y.x, sc);
+          nf.z.x = fmul(nf.z.x, sc);
+          nf.w.x = fmul(nf.w.x, sc);
+        }
+        if (total.y > dc.y) {
+          const float sc = scale_factor(dc.y, total.y);
+          nf.x.y = fmul(nf.x.y, sc);
+          nf.y.y = fmul(nf.y.y, sc);
+          nf.z.y = fmul(nf.z.y, sc);
+          nf.w.y = fmul(nf.w.y, sc);
+        }
+      }
+      if constexpr (F16) {
+        nf.x = quantize_f16x2(nf.x, fscale2, finv2);
+        nf.y = quantize_f16x2(nf.y, fscale2, finv2);
+        nf.z = quantize_f16x2(nf.z, fscale2, finv2);
+        nf.w = quantize_f16x2(nf.w, fscale2, finv2);
+      }
+      if constexpr (!INTERIOR) {  // cells off the grid keep zero outflow
+        if (!ys_in) nf = zero_flux();
+        if (!in0) nf.x.x = nf.y.x = nf.z.x = nf.w.x = 0.0f;
+        if (!in1) nf.x.y = nf.y.y = nf.z.y = nf.w.y = 0.0f;
+      }
+
+      // -- depth and flow map of row ys - 1, flowApply.comp:32-52
+      const int yd = ys - 1;
+      const Flux2 own = N1[s];
+      const float2 X1 = make_float2(own.y.y, __shfl_down_sync(0xffffffffu, own.y.x, 1));
+      const float2 X0 = make_float2(__shfl_up_sync(0xffffffffu, own.x.y, 1), own.x.x);
+      const float2 Y1 = nf.w, Y0 = N2[s].z;
+      const float2 in = fadd2(fadd2(fadd2(X1, X0), Y1), Y0);
+      const float2 out = fadd2(fadd2(fadd2(own.x, own.y), own.z), own.w);
+      const float2 dn = max0x2(sum_products(D0[s], fmul2(fsub2(in, out), cc2)));
+      const Flux2 handoff = N2[s];  // new outflow of row ys - 2: level s + 1's input
+      const float2 b_d = B0[s];     // terrain of the depth row
+      // shift the windows
+      H0[s] = hc;
+      H1[s] = hp;
+      D0[s] = D1[s];
+      D1[s] = d_in;
+      B0[s] = B1[s];
+      B1[s] = b_in;
+      N2[s] = own;
+      N1[s] = nf;
+      if (s + 1 < K) {
+        // level s + 1's input row yd: next step's sources, h = d + b
+        const bool yd_in = INTERIOR || (yd >= 0 && yd < H);
+        float2 dnext = dn;
+        if constexpr (!INTERIOR) {
+          if (!yd_in) dnext = z2;
+          if (!in0) dnext.x = 0.0f;
+          if (!in1) dnext.y = 0.0f;
+        }
+        dnext = sources2(dnext, yd);
+        d_in = dnext;
+        h_in = fadd2(dnext, b_d);
+        b_in = b_d;
+        f_in = handoff;
+      } else if (yd >= y0 && yd < y0 + R && out_lane && (INTERIOR || yd < H)) {
+        // the last level: depth, flux and flow map of row yd go out
+        const size_t g = (size_t)yd * pitch + (size_t)gx0;
+        const float2 vx = fsub2(fsub2(X1, own.x), fsub2(X0, own.y));
+        const float2 vy = fsub2(fsub2(Y1, own.z), fsub2(Y0, own.w));
+        if (INTERIOR || in1) {
+          *reinterpret_cast<float2*>(a.d_out + g) = dn;
+          *reinterpret_cast<float4*>(a.v_out + g) = make_float4(vx.x, vy.x, vx.y, vy.y);
+          if constexpr (F16) {
+            const __half2 p0 = __float22half2_rn(fmul2(make_float2(own.x.x, own.y.x), fscale2));
+            const __half2 q0 = __float22half2_rn(fmul2(make_float2(own.z.x, own.w.x), fscale2));
+            const __half2 p1 = __float22half2_rn(fmul2(make_float2(own.x.y, own.y.y), fscale2));
+            const __half2 q1 = __float22half2_rn(fmul2(make_float2(own.z.y, own.w.y), fscale2));
+            uint4 packed;
+            packed.x = *reinterpret_cast<const uint32_t*>(&p0);
+            packed.y = *reinterpret_cast<const uint32_t*>(&q0);
+            packed.z = *reinterpret_cast<const uint32_t*>(&p1);
+            packed.w = *reinterpret_cast<const uint32_t*>(&q1);
+            *reinterpret_cast<uint4*>(reinterpret_cast<uint2*>(a.f_out) + g) = packed;
+          } else {
+            float4* fo = reinterpret_cast<float4*>(a.f_out) + g;
+            fo[0] = make_float4(own.x.x, own.y.x, own.z.x, own.w.x);
+            fo[1] = make_float4(own.x.y, own.y.y, own.z.y, own.w.y);
+          }
+        } else if (in0) {  // the grid's last column (odd width)
+          a.d_out[g] = dn.x;
+          a.v_out[g] = make_float2(vx.x, vy.x);
+          if constexpr (F16) {
+            const __half2 p0 = __float22half2_rn(fmul2(make_float2(own.x.x, own.y.x), fscale2));
+            const __half2 q0 = __float22half2_rn(fmul2(make_float2(own.z.x, own.w.x), fscale2));
+            uint2 packed;
+            packed.x = *reinterpret_cast<const uint32_t*>(&p0);
+            packed.y = *reinterpret_cast<const uint32_t*>(&q0);
+            reinterpret_cast<uint2*>(a.f_out)[g] = packed;
+          } else {
+            reinterpret_cast<float4*>(a.f_out)[g] =
+                make_float4(own.x.x, own.y.x, own.z.x, own.w.x);
+          }
+        }
+      }
+    }
+  }
+  copy_wait<0>();
+}
+
+template <int K, bool F16, int P>
+__global__ void __launch_bounds__(kSweepThreads, (K <= 2 ? 4 : (K == 3 ? 3 : 2)))
+    sweep_kernel(const float* __restrict__ b, const float* __restrict__ d,
+                 const void* __restrict__ f, const __grid_constant__ StepArgs a, int R) {
+  using RG = SweepRing<F16, P>;
+  constexpr int VALID = kSweepCols - 4 * K;
+  extern __shared__ __align__(128) unsigned char sweep_smem[];
+  const int warp = threadIdx.x >> 5;
+  const int strips = (a.W + VALID - 1) / VALID;
+  const int bands = (a.H + R - 1) / R;
+  const int unit = blockIdx.x * kSweepWarps + warp;
+  // the previous launch on the stream has completed and its writes are
+  // visible before any global access (programmatic dependent launch)
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  if (unit >= strips * bands) return;  // the whole warp
+  const int xo = (unit % strips) * VALID;
+  const int y0 = (unit / strips) * R;
+  const int xs = xo - 2 * K;
+  uint32_t mask = 0;
+#pragma unroll
+  for (int k = 0; k < TWS_MAX_SOURCES; ++k) {
+    if (k < a.nsrc) {
+      const DevSource& s = a.src[k];
+      if (s.bx1 >= xs && s.bx0 < xs + kSweepCols && s.by1 >= y0 - 2 * K &&
+          s.by0 < y0 + R + 2 * K)
+        mask |= 1u << k;
+    }
+  }
+  unsigned char* ring = sweep_smem + warp * RG::WARP;
+  const bool interior =
+      xs >= 0 && xs + kSweepCols <= a.W && y0 - 2 * K >= 0 && y0 + R + 2 * K <= a.H;
+  if (interior)
+    sweep_unit<K, F16, true, P>(a, b, d, f, ring, xs, y0, R, mask);
+  else
+    sweep_unit<K, F16, false, P>(a, b, d, f, ring, xs, y0, R, mask);
+}
+
+template <int K, int P>
+const void* sweep_fn(int flux_storage) {
+  return flux_storage == TWS_FLUX_F16 ? reinterpret_cast<const void*>(&sweep_kernel<K, true, P>)
+                                      : reinterpret_cast<const void*>(&sweep_kernel<K, false, P>);
+}
+
+}  // namespace
+
+int sweep_valid_columns(int k) { return kSweepCols - 4 * k; }
+
+size_t sweep_smem_bytes(int flux_storage, int ring) {
+  return (size_t)kSweepWarps * ring * (flux_storage == TWS_FLUX_F16 ? SweepRing<true, 1>::ROW
+                                                                    : SweepRing<false, 1>::ROW);
+}
+
+cudaError_t launch_sweep_step(int k, int rows, int ring, int flux_storage, const float* b,
+                              const float* d, const void* f, const StepArgs& a, cudaStream_t s) {
+  const void* fn = nullptr;
+  if (ring != 4) return cudaErrorInvalidValue;
+  switch (k) {
+    case 2: fn = sweep_fn<2, 4>(flux_storage); break;
+    case 3: fn = sweep_fn<3, 4>(flux_storage); break;
+    case 4: fn = sweep_fn<4, 4>(flux_storage); break;
+    default: return cudaErrorInvalidValue;
+  }
+  if (rows < 1) return cudaErrorInvalidValue;
+  const int valid = kSweepCols - 4 * k;
+  const long long strips = (a.W + valid - 1) / valid, bands = (a.H + rows - 1) / rows;
+  const long long blocks = (strips * bands + kSweepWarps - 1) / kSweepWarps;
+  if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  const size_t smem = sweep_smem_bytes(flux_storage, ring);
+  if (smem > 48 * 1024) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3((unsigned)blocks);
+  cfg.blockDim = dim3(kSweepThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  using Fn = void (*)(const float*, const float*, const void*, StepArgs, int);
+  const cudaError_t e =
+      cudaLaunchKernelEx(&cfg, reinterpret_cast<Fn>(const_cast<void*>(fn)), b, d, f, a, rows);
+  count_launch();
+  return e;
+}
+
+}  // namespace tws

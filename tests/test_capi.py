@@ -123,12 +123,20 @@ def test_binding_raises_when_library_missing(tmp_path, monkeypatch):
 def test_variant_table(tws):
     v = tws.variants()
     assert len(v) >= 4
-    assert {k for k, _, _, _, _ in v} == {1, 2, 3, 4}
-    for k, tx, ty, stages, smem in v:
+    assert {k for k, _, _, _, _, _ in v} == {1, 2, 3, 4}
+    for k, tx, ty, stages, smem, kind in v:
         # TMA tile variants stage whole 16-byte units in shared memory; the
-        # register-streaming variants (30-column strips) use none
+        # register-streaming variants (30-column strips) use none; the sweeps
+        # yield 64 - 4K columns per warp strip and stage rows in shared memory
         assert ty >= 1 and stages in (1, 2) and 0 <= smem <= 227 * 1024
-        assert (smem > 0 and tx % 4 == 0) or (smem == 0 and tx == 30 and k == 1)
+        if kind == tws.VARIANT_TILE:
+            assert smem > 0 and tx % 4 == 0
+        elif kind == tws.VARIANT_STREAM:
+            assert smem == 0 and tx == 30 and k == 1
+        else:
+            assert kind == tws.VARIANT_SWEEP and 2 <= k <= 4 and tx == 64 - 4 * k and smem > 0
+    assert any(x[5] == tws.VARIANT_SWEEP for x in v)
+    assert tws.lib().tws_variant_kind(len(v)) == tws.ERR_INVALID
     # entries 0..3 are the defaults for K = 1..4
     assert [v[i][0] for i in range(4)] == [1, 2, 3, 4]
     assert tws.lib().tws_variant_info(len(v), None, None, None, None, None) == tws.ERR_INVALID

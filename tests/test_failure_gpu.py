@@ -32,7 +32,7 @@ def _tile_variants(tws):
     """Tile variants (those that stage tiles in shared memory): the first
     K=1 and K=2 one-CTA-per-tile variants, the first persistent one and the
     last one in the table."""
-    tiled = [(i, v) for i, v in enumerate(tws.variants()) if v[4] > 0]
+    tiled = [(i, v) for i, v in enumerate(tws.variants()) if v[5] == tws.VARIANT_TILE]
     picks = [next(i for i, v in tiled if v[0] == 1 and v[3] == 1),
              next(i for i, v in tiled if v[0] == 2 and v[3] == 1),
              next(i for i, v in tiled if v[3] == 2),

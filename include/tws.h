@@ -84,7 +84,10 @@ TWS_API int tws_params_reference(float steps_per_second, float flow_damping,
 
 /* A water source.  DISK (the benchmark's rain): every cell whose integer
  * offset (x-cx, y-cy) satisfies dx*dx+dy*dy <= radius*radius gains `rate`
- * metres (cx, cy, radius are whole cells).  BRUSH (the reference's brush,
+ * metres (cx, cy, radius are whole cells).  The FP32 sum d + rate is rounded
+ * without bias: down or up to a neighbouring float with the probability that
+ * makes its expectation exact, decided by a hash of the cell and the bits of
+ * d (deterministic), so long rainy runs conserve volume.  BRUSH (the reference's brush,
  * waterBrush.comp:26-28): d += saturate(1 - |(cx,cy)-(x,y)|^2 / radius) * rate,
  * where radius holds BrushSizeSq and rate BrushIntensity. */
 typedef struct tws_source {

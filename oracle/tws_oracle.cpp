@@ -110,10 +110,49 @@ inline int num_threads(int requested) {
 #endif
 }
 
-// Source term.  DISK follows the benchmark's uniform rain disk; BRUSH follows
-// waterBrush.comp:26-28: toBrush = BrushPos - gridPosition; q = dot / S;
-// d += saturate(1 - q) * I.  Cells where the increment is zero are left as
-// they are (d + 0 == d for every d >= +0, the only depths the step produces).
+// The integer hash "lowbias32" (C. Wellons, hash-prospector: xorshift-multiply,
+// constants 0x7feb352d and 0x846ca68b).
+inline uint32_t rain_hash32(uint32_t v) {
+  v ^= v >> 16;
+  v *= 0x7feb352du;
+  v ^= v >> 15;
+  v *= 0x846ca68bu;
+  v ^= v >> 16;
+  return v;
+}
+
+// d + rate for the DISK rain on FP32 depths, rounded without bias.  Round to
+// nearest alone biases a 0.01 m increment by a fixed fraction of an ulp of d
+// (+0.24 ulp on 8-16 m, -0.44 on 32-64 m, ...), so the total volume drifts by
+// up to about 2e-4 of the rain.  Here the exact rounding error e of s = d + r
+// comes from TwoSum (Knuth), and s moves one ulp toward d + r when
+// u * |step| < |e|, with u in [0, 1) from a hash of the cell and the bits of
+// d: the expected result is d + r exactly.  Every operation is exact or
+// IEEE round-to-nearest, so the GPU kernels reproduce it bit for bit.  The
+// FP64 path adds plainly (its rounding is far below what is measured).
+inline float add_rain(float d, float r, int x, int y) {
+  const float s = d + r;
+  const float bp = s - d;
+  const float e = (d - (s - bp)) + (r - bp);
+  if (e == 0.0f) return s;
+  uint32_t sb, db;
+  std::memcpy(&sb, &s, 4);
+  std::memcpy(&db, &d, 4);
+  sb = ((s > 0.0f) == (e > 0.0f)) ? sb + 1u : sb - 1u;  // the neighbour toward d + r
+  float next;
+  std::memcpy(&next, &sb, 4);
+  const float step = next - s;
+  const uint32_t h = rain_hash32(db ^ rain_hash32((uint32_t)x ^ rain_hash32((uint32_t)y)));
+  const float u = (float)(h >> 8) * 0x1p-24f;
+  return (u * std::fabs(step) < std::fabs(e)) ? next : s;
+}
+inline double add_rain(double d, double r, int, int) { return d + r; }
+
+// Source term.  DISK follows the benchmark's uniform rain disk (add_rain);
+// BRUSH follows waterBrush.comp:26-28: toBrush = BrushPos - gridPosition;
+// q = dot / S; d += saturate(1 - q) * I.  Cells where the increment is zero
+// are left as they are (d + 0 == d for every d >= +0, the only depths the
+// step produces).
 template <class T>
 void apply_sources(int W, int H, T* d, const tws_oracle_source* src, int nsrc, int nth) {
   for (int k = 0; k < nsrc; ++k) {
@@ -128,7 +167,8 @@ void apply_sources(int W, int H, T* d, const tws_oracle_source* src, int nsrc, i
       for (int y = y0; y <= y1; ++y)
         for (int x = x0; x <= x1; ++x) {
           const long long dx = x - cx, dy = y - cy;
-          if (dx * dx + dy * dy <= r2) d[(size_t)y * W + x] = d[(size_t)y * W + x] + rate;
+          if (dx * dx + dy * dy <= r2)
+            d[(size_t)y * W + x] = add_rain(d[(size_t)y * W + x], rate, x, y);
         }
     } else {
       const T bx = (T)s.cx, by = (T)s.cy, S = (T)s.radius, I = (T)s.rate;

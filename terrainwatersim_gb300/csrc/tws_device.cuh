@@ -68,6 +68,39 @@ __device__ __forceinline__ float saturate01(float v) {
 }
 
 // ---- the source term -----------------------------------------------------------
+// The integer hash "lowbias32" (C. Wellons, hash-prospector: xorshift-multiply,
+// constants 0x7feb352d and 0x846ca68b).
+__device__ __forceinline__ uint32_t rain_hash32(uint32_t v) {
+  v ^= v >> 16;
+  v *= 0x7feb352du;
+  v ^= v >> 15;
+  v *= 0x846ca68bu;
+  v ^= v >> 16;
+  return v;
+}
+
+// d + r for the DISK rain, rounded without bias.  Round to nearest alone
+// biases a 0.01 m increment by a fixed fraction of an ulp of d (+0.24 ulp on
+// 8-16 m, -0.44 on 32-64 m, ...), and the total volume of a long rainy run
+// drifts with it (up to about 2e-4 of the rain).  TwoSum (Knuth) gives the
+// exact rounding error e of s = d + r; s moves one ulp toward d + r when
+// u * |step| < |e|, with u in [0, 1) a hash of the cell and the bits of d.
+// The expected result is d + r exactly, the run stays deterministic, and
+// every operation is exact or IEEE round-to-nearest, as in the oracle.
+__device__ __forceinline__ float add_rain(float d, float r, int x, int y) {
+  const float s = fadd(d, r);
+  const float bp = fsub(s, d);
+  const float e = fadd(fsub(d, fsub(s, bp)), fsub(r, bp));
+  if (e == 0.0f) return s;
+  const uint32_t sb = __float_as_uint(s);
+  const float next = __uint_as_float(((s > 0.0f) == (e > 0.0f)) ? sb + 1u : sb - 1u);
+  const float step = fsub(next, s);
+  const uint32_t h = rain_hash32(__float_as_uint(d) ^
+                                 rain_hash32((uint32_t)x ^ rain_hash32((uint32_t)y)));
+  const float u = fmul(__uint2float_rn(h >> 8), 0x1p-24f);
+  return (fmul(u, fabsf(step)) < fabsf(e)) ? next : s;
+}
+
 // Not inlined: only tiles that a source touches call it, and an inlined copy
 // in every unrolled cell loop of the tile kernels would multiply their code
 // size past the instruction cache.
@@ -80,7 +113,7 @@ static __device__ __noinline__ float add_sources(float d, int gx, int gy, const 
     if (gx < s.bx0 || gx > s.bx1 || gy < s.by0 || gy > s.by1) continue;
     if (s.kind == TWS_SOURCE_DISK) {
       const long long dx = gx - s.icx, dy = gy - s.icy;
-      if (dx * dx + dy * dy <= (long long)s.ir * s.ir) d = fadd(d, s.rate);
+      if (dx * dx + dy * dy <= (long long)s.ir * s.ir) d = add_rain(d, s.rate, gx, gy);
     } else {
       const float tx = fsub(s.cx, (float)gx), ty = fsub(s.cy, (float)gy);
       const float q = fdiv(fadd(fmul(tx, tx), fmul(ty, ty)), s.radius);

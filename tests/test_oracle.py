@@ -294,3 +294,31 @@ def test_oracle_surface_matches_reference_render_live(oracle, N, seed):
         assert not np.isnan(want[k]).any(), k  # every sample was a texel centre
         assert_bitexact(got[k], want[k], k)
     assert np.array_equal(got["dry"], want["dry"])
+
+
+# ---------------------------------------------------------------- DISK rain rounding
+
+@pytest.mark.parametrize("depth", [3.0, 12.0, 20.0, 40.0, 100.0])
+def test_disk_rain_rounding_is_unbiased(oracle, depth):
+    """Round to nearest biases d + 0.01 by a fixed fraction of an ulp of d in
+    each binade (+2.3e-5 of the rain on 8-32 m, -1.7e-4 on 32-64 m); the DISK
+    source's unbiased rounding adds the rate exactly in expectation, and is
+    deterministic."""
+    N, reps = 64, 400
+    d = np.full((N, N), np.float32(depth))
+    rate = np.float32(0.01)
+    src = [(oracle.SOURCE_DISK, 32, 32, 100, 0.01)]  # every cell
+    d2 = d.copy()
+    for _ in range(reps):
+        oracle.sources_f32(d, src)
+        oracle.sources_f32(d2, src)
+    assert_bitexact(d, d2, "determinism")
+    added = float(np.sum(d, dtype=np.float64) - N * N * float(np.float32(depth)))
+    want = reps * N * N * float(rate)
+    # round to nearest on the same adds, for scale
+    rn = np.full((N, N), np.float32(depth))
+    for _ in range(reps):
+        rn = (rn + rate).astype(np.float32)
+    rn_bias = abs(float(np.sum(rn, dtype=np.float64)) - N * N * float(np.float32(depth)) - want)
+    assert abs(added - want) / want < 2e-6, (added, want)
+    assert abs(added - want) < 0.1 * rn_bias or rn_bias == 0.0

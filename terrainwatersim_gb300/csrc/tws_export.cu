@@ -228,7 +228,7 @@ __global__ void export_mip1_kernel4(const float* __restrict__ b, const float* __
     }
   }
   // level 1 texel (x/2 + j, y/2) from cells (x + 2j, y), (x + 2j + 1, y),
-  // (x + 2j, y + 1), (x + 2j + 1, y + 1), in mip_kernel's order
+  // (x + 2j, y + 1), (x + 2j + 1, y + 1), in the order of mip_chain_kernel's filter
   const size_t m = (size_t)(y / 2) * (W / 2) + x / 2;
 #pragma unroll
   for (int j = 0; j < 2; ++j) {
@@ -260,16 +260,51 @@ __device__ __forceinline__ float avg4(float a, float b, float c, float d) {
   return fmul(fadd(fadd(a, b), fadd(c, d)), 0.25f);
 }
 
-__global__ void mip_kernel(const float4* __restrict__ src, int sw, float4* __restrict__ dst,
-                           int dw, int dh) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  if (x >= dw || y >= dh) return;
-  const float4 a = src[(size_t)(2 * y) * sw + 2 * x], b = src[(size_t)(2 * y) * sw + 2 * x + 1];
-  const float4 c = src[(size_t)(2 * y + 1) * sw + 2 * x],
-               e = src[(size_t)(2 * y + 1) * sw + 2 * x + 1];
-  dst[(size_t)y * dw + x] = make_float4(avg4(a.x, b.x, c.x, e.x), avg4(a.y, b.y, c.y, e.y),
-                                        avg4(a.z, b.z, c.z, e.z), avg4(a.w, b.w, c.w, e.w));
+// Up to kMipChain levels of the mip pyramid in one launch.  A CTA loads a
+// 32 x 32 texel block of the source level into shared memory and halves it
+// level by level with the 2 x 2 filter ((a + b) + (c + e)) * 0.25 (a, b the
+// upper texel pair, c, e the lower), writing each level's texels of
+// the block.  Level l + m texel q depends only on source texels
+// [q 2^m, (q + 1) 2^m), so every texel of a level of floor(w / 2^m) texels
+// is made from texels of this block inside the source; texels past a
+// level's edge are computed from zero fill and not written.
+constexpr int kMipBlock = 32;
+constexpr int kMipChain = 5;  // 32 -> 16 -> 8 -> 4 -> 2 -> 1
+struct MipChain {
+  float4* dst[kMipChain];
+  int w[kMipChain], h[kMipChain];  // sizes of the levels written
+  int n;                           // levels written, 1 .. kMipChain
+};
+
+__global__ void __launch_bounds__(256)
+    mip_chain_kernel(const float4* __restrict__ src, int sw, int sh, MipChain c) {
+  __shared__ float4 buf[2][kMipBlock * kMipBlock];
+  const int bx = blockIdx.x * kMipBlock, by = blockIdx.y * kMipBlock;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < kMipBlock * kMipBlock; i += blockDim.x) {
+    const int x = bx + (i % kMipBlock), y = by + (i / kMipBlock);
+    buf[0][i] = (x < sw && y < sh) ? src[(size_t)y * sw + x] : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  __syncthreads();
+  int side = kMipBlock;
+  for (int l = 0; l < c.n; ++l) {
+    const int half = side / 2;
+    const float4* in = buf[l & 1];
+    float4* out = buf[(l + 1) & 1];
+    const int ox = bx >> (l + 1), oy = by >> (l + 1);  // the block's origin in this level
+    for (int i = tid; i < half * half; i += blockDim.x) {
+      const int x = i % half, y = i / half;
+      const float4 a = in[(2 * y) * side + 2 * x], b = in[(2 * y) * side + 2 * x + 1];
+      const float4 cc = in[(2 * y + 1) * side + 2 * x], e = in[(2 * y + 1) * side + 2 * x + 1];
+      const float4 r = make_float4(avg4(a.x, b.x, cc.x, e.x), avg4(a.y, b.y, cc.y, e.y),
+                                   avg4(a.z, b.z, cc.z, e.z), avg4(a.w, b.w, cc.w, e.w));
+      out[y * half + x] = r;
+      const int gx = ox + x, gy = oy + y;
+      if (gx < c.w[l] && gy < c.h[l]) c.dst[l][(size_t)gy * c.w[l] + gx] = r;
+    }
+    __syncthreads();
+    side = half;
+  }
 }
 
 dim3 grid2d(int w, int h) { return dim3((w + 31) / 32, (h + 7) / 8); }
@@ -324,7 +359,7 @@ cudaError_t launch_export(const float* b, const float* d, const float2* v, int W
       count_launch();
     }
   }
-  if (terrain_rgba) {
+  if (terrain_rgba && mips) {
     const float4* src = reinterpret_cast<const float4*>(terrain_rgba);
     float4* dst = reinterpret_cast<float4*>(mips);
     int sw = W, sh = H, l = 1;
@@ -335,15 +370,29 @@ cudaError_t launch_export(const float* b, const float* d, const float2* v, int W
       sh = H / 2;
       l = 2;
     }
-    for (; l <= mip_levels && mips; ++l) {
-      const int dw = sw / 2 > 0 ? sw / 2 : 1, dh = sh / 2 > 0 ? sh / 2 : 1;
-      if (sw < 2 || sh < 2) break;
-      mip_kernel<<<grid2d(dw, dh), dim3(32, 8), 0, s>>>(src, sw, dst, dw, dh);
+    // the remaining levels, up to kMipChain per launch (4096^2: 3 launches
+    // for levels 2..12 instead of 11)
+    while (l <= mip_levels && sw >= 2 && sh >= 2) {
+      MipChain c{};
+      int w = sw, h = sh;
+      float4* p = dst;
+      while (c.n < kMipChain && l + c.n <= mip_levels && w >= 2 && h >= 2) {
+        w /= 2;
+        h /= 2;
+        c.dst[c.n] = p;
+        c.w[c.n] = w;
+        c.h[c.n] = h;
+        p += (size_t)w * h;
+        ++c.n;
+      }
+      const dim3 grid((sw + kMipBlock - 1) / kMipBlock, (sh + kMipBlock - 1) / kMipBlock);
+      mip_chain_kernel<<<grid, 256, 0, s>>>(src, sw, sh, c);
       count_launch();
-      src = dst;
-      dst += (size_t)dw * dh;
-      sw = dw;
-      sh = dh;
+      src = c.dst[c.n - 1];
+      sw = c.w[c.n - 1];
+      sh = c.h[c.n - 1];
+      dst = p;
+      l += c.n;
     }
   }
   return cudaGetLastError();

@@ -94,22 +94,28 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def ncu_traffic_per_cell(k: int, flux: str):
+def ncu_traffic_per_cell(k: int, flux: str, variant: int | None = None):
     """DRAM bytes per cell per launch of the step kernel from the committed ncu
-    summary (profiles/step_kernel_traffic.txt), or None."""
+    summary (profiles/step_kernel_traffic.txt): the line of this variant, else
+    of the same temporal depth and flux storage; None if there is none."""
     path = os.path.join(ROOT, "profiles", "step_kernel_traffic.txt")
     if not os.path.exists(path):
         return None
+    by_k = None
     for line in open(path):
         if line.startswith("#") or "=" not in line:
             continue
         kv = dict(tok.split("=", 1) for tok in line.split() if "=" in tok)
         try:
-            if int(kv["k"]) == k and kv.get("flux", "f32") == flux:
-                return float(kv["dram_bytes_per_launch"]) / float(kv["cells"])
+            if int(kv["k"]) != k or kv.get("flux", "f32") != flux:
+                continue
+            per_cell = float(kv["dram_bytes_per_launch"]) / float(kv["cells"])
+            if variant is not None and int(kv.get("variant", -1)) == variant:
+                return per_cell
+            by_k = per_cell if by_k is None else by_k
         except (KeyError, ValueError):
             continue
-    return None
+    return by_k
 
 
 class ClockSampler:
@@ -310,7 +316,7 @@ def run_ours(args):
     compulsory = bpc * cells
     achieved = compulsory / launch_s / 1e9
     effective = bpc * cell_steps_per_launch / launch_s / 1e9
-    tpc = ncu_traffic_per_cell(best_k, args.flux)
+    tpc = ncu_traffic_per_cell(best_k, args.flux, best_v)
     plain = variants.get(0)
     if plain is None:  # no sweep: time the plain kernel alone for its top-level keys
         g.generate_scene(2026, 40.0, 15.0)
@@ -432,6 +438,17 @@ def run_ours(args):
                 "kernel": f"{kernel_name(vinfo[best_v])}<K={best_k},"
                           f"{vinfo[best_v][1]}x{vinfo[best_v][2]}>",
             },
+            "roofline_by_kernel": {
+                (f"{i}_{kernel_name(vinfo[i])}_k{vinfo[i][0]}_{vinfo[i][1]}x{vinfo[i][2]}"): {
+                    "launch_us": round(v["seconds"] / max(1, v["launches"]) * 1e6, 2),
+                    "frac": round(bpc * cells / (v["seconds"] / max(1, v["launches"])) / 1e9
+                                  / peak, 4),
+                } for i, v in variants.items() if i in (0, 16, best_v)},
+            "roofline_note": "frac = compulsory bytes (the state in and out once) per launch / "
+                             "launch time / measured copy rate; a kernel advancing K steps per "
+                             "launch moves the state once for K steps, so a faster deep kernel "
+                             "can show a lower frac (the K = 3 sweep is bound by instruction "
+                             "latency, not HBM: profiles/sweep_kernel_k3_40rows_4096.md)",
             "variants": {
                 (f"{i}_{'plain' if vinfo[i][0] == 1 else 'blocked_k%d' % vinfo[i][0]}"
                  f"_{vinfo[i][1]}x{vinfo[i][2]}_{variant_form(vinfo[i])}"): {

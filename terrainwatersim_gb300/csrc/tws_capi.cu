@@ -57,6 +57,7 @@ struct tws_grid {
   double* vol_out = nullptr;
   double vol_host[1] = {0.0};
   int* err = nullptr;     // device error word
+  int* queue = nullptr;   // the sweep kernel's work queue (two ints, zero between launches)
   int err_host[1] = {0};
   CUtensorMap* desc = nullptr;  // device copies of the maps, 5 per variant (batched kernel)
   long long wait_cycles = kDefaultWaitCycles;  // SM clocks a tile-load wait may take
@@ -184,6 +185,10 @@ int chosen_variant(const tws_grid* g) {
     const Tuned t = tuned_lookup(g);
     if (t.variant >= 0) return t.variant;
   }
+  if (g->steps_per_launch == 0 && (long long)g->W * g->H >= kLargeGridCells) {
+    const int v = step_variant_large_grid(g->flux_storage);
+    if (v >= 0) return v;
+  }
   const int k = g->steps_per_launch > 0 ? g->steps_per_launch : default_steps_per_launch(g);
   return step_variant_for(k, g->flux_storage);
 }
@@ -227,6 +232,7 @@ StepArgs make_step_args(const tws_grid* g) {
   a.flux_scale = g->flux_scale;
   a.flux_inv_scale = 1.0f / g->flux_scale;
   a.err = g->err;
+  a.queue = g->queue;
   a.wait_cycles = g->wait_cycles;
   a.drop_loads = g->drop_loads;
   return a;
@@ -385,7 +391,7 @@ TWS_API int tws_create(int width, int height, const tws_sim_params* params, int 
   const size_t ob = take(n * 4), od0 = take(n * 4), od1 = take(n * 4), of0 = take(n * fb),
                of1 = take(n * fb), ov = take(n * 8),
                op = take(sizeof(double) * volume_partials_needed()), oo = take(sizeof(double)),
-               oe = take(sizeof(int)), ot = take(sizeof(CUtensorMap) * 5 * step_variant_count());
+               oe = take(64), ot = take(sizeof(CUtensorMap) * 5 * step_variant_count());
   cudaMemPool_t pool = library_pool(g->device);
   if (!pool || cudaMallocFromPoolAsync(reinterpret_cast<void**>(&g->slab), off, pool, g->stream) !=
                    cudaSuccess) {
@@ -401,6 +407,7 @@ TWS_API int tws_create(int width, int height, const tws_sim_params* params, int 
   g->vol_partials = reinterpret_cast<double*>(g->slab + op);
   g->vol_out = reinterpret_cast<double*>(g->slab + oo);
   g->err = reinterpret_cast<int*>(g->slab + oe);
+  g->queue = reinterpret_cast<int*>(g->slab + oe + 16);
   g->desc = reinterpret_cast<CUtensorMap*>(g->slab + ot);
   // Zero everything, padding included (the F16 flux map reads the padding
   // cell of odd-width rows and relies on it staying zero).
@@ -410,7 +417,7 @@ TWS_API int tws_create(int width, int height, const tws_sim_params* params, int 
   cudaMemsetAsync(g->f[0], 0, n * fb, g->stream);
   cudaMemsetAsync(g->f[1], 0, n * fb, g->stream);
   cudaMemsetAsync(g->v, 0, n * 8, g->stream);
-  cudaMemsetAsync(g->err, 0, sizeof(int), g->stream);
+  cudaMemsetAsync(g->err, 0, 64, g->stream);  // the error word and the sweep queue
   if (cudaStreamSynchronize(g->stream) != cudaSuccess) return bail(TWS_ERR_CUDA);
   *out = g;
   return TWS_OK;

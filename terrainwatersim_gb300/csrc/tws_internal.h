@@ -37,6 +37,8 @@ struct StepArgs {
   int* err;              // device error word (bounded-wait time-outs)
   long long wait_cycles; // bounded waits give up after this many SM clocks
   int drop_loads;        // test hook: tile loads arm their barrier but issue no copy
+  int* queue;            // the sweep kernel's work queue: next unit, warps done (zero
+                         // between launches; the last warp of a launch resets it)
 };
 
 // Kernel variants (temporal block depth K x tile).
@@ -108,6 +110,9 @@ constexpr long long kDefaultWaitCycles = 4000000000LL;
 int step_variant_count();
 const StepVariant& step_variant(int i);
 int step_variant_for(int k, int flux_storage);
+// The automatic choice for grids of at least kLargeGridCells cells, or -1.
+constexpr long long kLargeGridCells = 12LL << 20;
+int step_variant_large_grid(int flux_storage);
 // Tile variants read through the tensor maps, stream variants through the
 // raw pointers (b, d, f of the current state).
 cudaError_t launch_step(int variant, int flux_storage, const CUtensorMap* tm_b,

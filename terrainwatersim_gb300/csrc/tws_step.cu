@@ -882,13 +882,17 @@ struct VariantTable {
     add<4, 32, 32, 1, true>();  // 20
     add<4, 64, 16, 1, true>();  // 21
     add<3, 64, 32, 1, true>();  // 22
-    // row sweeps: 64-column warp strips, K time levels in registers
-    // (4096^2: 32-row bands beat 64- and 128-row ones, 16-row bands pay too
-    // much halo; a ring of 8 rows is no faster than 4)
+    // row sweeps: 64-column warp strips, K time levels in registers.  4096^2
+    // FP32 (Gcell-steps/s): K = 3 with 40-row bands 199.7, 48 195.0, 32 194.1,
+    // 64 186.8, 96 175.6, 128 168.4; K = 2 172 with 24-48-row bands; K = 4
+    // 162 with 64-row bands.  A ring of 8 rows is no faster than 4.
     add_sweep(2, 32, 4);   // 23
-    add_sweep(3, 32, 4);   // 24
-    add_sweep(3, 64, 4);   // 25
-    add_sweep(4, 32, 4);   // 26
+    add_sweep(2, 48, 4);   // 24
+    add_sweep(3, 32, 4);   // 25
+    add_sweep(3, 40, 4);   // 26  the default for large FP32 grids
+    add_sweep(3, 48, 4);   // 27
+    add_sweep(3, 64, 4);   // 28
+    add_sweep(4, 64, 4);   // 29
   }
   void add_sweep(int k, int rows, int ring) {
     VariantEntry s{};
@@ -948,6 +952,21 @@ EncodeTiledFn encode_fn(std::string* why) {
 
 int step_variant_count() { return table().n; }
 const StepVariant& step_variant(int i) { return table().e[i].v; }
+
+int step_variant_large_grid(int flux_storage) {
+  // FP32 flux on large grids: the three-step row sweep with 40-row bands
+  // (4096^2: 199.7 against 192.2 for the two-step tiles; with FP16 storage
+  // and on smaller grids the tiles are faster)
+  if (flux_storage != TWS_FLUX_F32) return -1;
+  static const int v = [] {
+    for (int i = 0; i < step_variant_count(); ++i) {
+      const StepVariant& e = step_variant(i);
+      if (e.kind == kKindSweep && e.k == 3 && e.ry == 40) return i;
+    }
+    return -1;
+  }();
+  return v;
+}
 
 int step_variant_for(int k, int /*flux_storage*/) {
   // Default variant per temporal depth (fastest per depth on 4096^2): the

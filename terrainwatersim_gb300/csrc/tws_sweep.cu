@@ -5,7 +5,8 @@
 // transcription of the shaders), organised so that no halo is recomputed in y:
 //
 // * A warp owns a strip of 64 columns (two per lane) and sweeps it down a
-//   band of R rows.  Each lane keeps, per time level s = 0..K-1, a rolling
+//   band of R rows; the warps are persistent and take (strip, band) units
+//   from a per-grid queue, border units first.  Each lane keeps, per time level s = 0..K-1, a rolling
 //   window of the rows that level needs in registers: surface heights h of
 //   three rows, depths and terrain of two rows, new outflows of two rows.
 //   Row by row, level s computes the outflow of one row and the depth of the
@@ -34,6 +35,10 @@
 // HBM traffic per launch: the state once in, once out (52 B per cell for FP32
 // flux, 36 B for FP16), plus the re-read of the strip and band overlaps,
 // which L2 serves when neighbouring strips run together.
+
+#include <algorithm>
+#include <map>
+#include <mutex>
 
 #include "tws_device.cuh"
 #include "tws_internal.h"
@@ -159,10 +164,30 @@ __device__ __forceinline__ void sweep_unit(const StepArgs& a, const float* __res
                    make_float2(c0.w, c1.w)};
     }
   };
+  // The sources of row r on this lane's two cells, in source order (as
+  // add_sources applies them).  A DISK is tested inline: an out-of-line call
+  // per cell and level made the warps under a rain disk several times slower
+  // than the rest, and with one wave of warps the launch waits for them.
   auto sources2 = [&](float2 dv, int r) -> float2 {
     if (!mask || !(INTERIOR || (r >= 0 && r < H))) return dv;
-    if (in0) dv.x = add_sources(dv.x, gx0, r, a, mask);
-    if (in1) dv.y = add_sources(dv.y, gx1, r, a, mask);
+#pragma unroll 1
+    for (int k = 0; k < a.nsrc; ++k) {
+      if (!((mask >> k) & 1u)) continue;
+      const DevSource& src = a.src[k];
+      if (r < src.by0 || r > src.by1) continue;  // warp-uniform
+      if (src.kind == TWS_SOURCE_DISK) {
+        const long long dy = r - src.icy;
+        const long long room = (long long)src.ir * src.ir - dy * dy;  // dx^2 allowed
+        const long long dx0 = gx0 - src.icx, dx1 = gx1 - src.icx;
+        if (in0 && gx0 >= src.bx0 && gx0 <= src.bx1 && dx0 * dx0 <= room)
+          dv.x = add_rain(dv.x, src.rate, gx0, r);
+        if (in1 && gx1 >= src.bx0 && gx1 <= src.bx1 && dx1 * dx1 <= room)
+          dv.y = add_rain(dv.y, src.rate, gx1, r);
+      } else {
+        if (in0) dv.x = add_sources(dv.x, gx0, r, a, 1u << k);
+        if (in1) dv.y = add_sources(dv.y, gx1, r, a, 1u << k);
+      }
+    }
     return dv;
   };
 
@@ -342,6 +367,37 @@ __device__ __forceinline__ void sweep_unit(const StepArgs& a, const float* __res
   copy_wait<0>();
 }
 
+// Queue position i -> (strip, band): the units on the grid's border first
+// (their cells take the slower edge path, and a launch ends with its slowest
+// units), then the interior strip by strip, band by band.
+__device__ __forceinline__ void sweep_unit_coords(int i, int S, int B, int& s, int& b) {
+  if (S < 3 || B < 3) {
+    s = i % S;
+    b = i / S;
+    return;
+  }
+  const int ne = 2 * S + 2 * (B - 2);
+  if (i < S) {
+    s = i;
+    b = 0;
+  } else if (i < 2 * S) {
+    s = i - S;
+    b = B - 1;
+  } else if (i < 2 * S + (B - 2)) {
+    s = 0;
+    b = 1 + (i - 2 * S);
+  } else if (i < ne) {
+    s = S - 1;
+    b = 1 + (i - 2 * S - (B - 2));
+  } else {
+    const int j = i - ne;
+    s = 1 + j % (S - 2);
+    b = 1 + j / (S - 2);
+  }
+}
+
+// Persistent warps (one wave): each takes units (strip, band) from the grid's
+// queue until none is left, so warps that drew cheap units take more of them.
 template <int K, bool F16, int P>
 __global__ void __launch_bounds__(kSweepThreads, (K <= 2 ? 4 : (K == 3 ? 3 : 2)))
     sweep_kernel(const float* __restrict__ b, const float* __restrict__ d,
@@ -349,35 +405,53 @@ __global__ void __launch_bounds__(kSweepThreads, (K <= 2 ? 4 : (K == 3 ? 3 : 2))
   using RG = SweepRing<F16, P>;
   constexpr int VALID = kSweepCols - 4 * K;
   extern __shared__ __align__(128) unsigned char sweep_smem[];
-  const int warp = threadIdx.x >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int strips = (a.W + VALID - 1) / VALID;
   const int bands = (a.H + R - 1) / R;
-  const int unit = blockIdx.x * kSweepWarps + warp;
-  // the previous launch on the stream has completed and its writes are
-  // visible before any global access (programmatic dependent launch)
+  const int total = strips * bands;
+  // the previous launch on the stream has completed and its writes (the
+  // state, and the queue it reset) are visible before any global access
+  // (programmatic dependent launch)
   asm volatile("griddepcontrol.wait;" ::: "memory");
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-  if (unit >= strips * bands) return;  // the whole warp
-  const int xo = (unit % strips) * VALID;
-  const int y0 = (unit / strips) * R;
-  const int xs = xo - 2 * K;
-  uint32_t mask = 0;
+  unsigned char* ring = sweep_smem + warp * RG::WARP;
+  for (;;) {
+    int u = 0;
+    if (lane == 0) u = atomicAdd(&a.queue[0], 1);
+    u = __shfl_sync(0xffffffffu, u, 0);
+    if (u >= total) break;  // the whole warp
+    int si, bi;
+    sweep_unit_coords(u, strips, bands, si, bi);
+    const int xs = si * VALID - 2 * K;
+    const int y0 = bi * R;
+    uint32_t mask = 0;
 #pragma unroll
-  for (int k = 0; k < TWS_MAX_SOURCES; ++k) {
-    if (k < a.nsrc) {
-      const DevSource& s = a.src[k];
-      if (s.bx1 >= xs && s.bx0 < xs + kSweepCols && s.by1 >= y0 - 2 * K &&
-          s.by0 < y0 + R + 2 * K)
-        mask |= 1u << k;
+    for (int k = 0; k < TWS_MAX_SOURCES; ++k) {
+      if (k < a.nsrc) {
+        const DevSource& s = a.src[k];
+        if (s.bx1 >= xs && s.bx0 < xs + kSweepCols && s.by1 >= y0 - 2 * K &&
+            s.by0 < y0 + R + 2 * K)
+          mask |= 1u << k;
+      }
+    }
+    const bool interior =
+        xs >= 0 && xs + kSweepCols <= a.W && y0 - 2 * K >= 0 && y0 + R + 2 * K <= a.H;
+    if (interior)
+      sweep_unit<K, F16, true, P>(a, b, d, f, ring, xs, y0, R, mask);
+    else
+      sweep_unit<K, F16, false, P>(a, b, d, f, ring, xs, y0, R, mask);
+  }
+  // The last warp to finish resets the queue for the next launch: every other
+  // warp has made its final claim by then, and the next launch reads the
+  // queue only after this grid has completed.
+  if (lane == 0) {
+    __threadfence();
+    if (atomicAdd(&a.queue[1], 1) == (int)(gridDim.x * kSweepWarps) - 1) {
+      a.queue[0] = 0;
+      a.queue[1] = 0;
+      __threadfence();
     }
   }
-  unsigned char* ring = sweep_smem + warp * RG::WARP;
-  const bool interior =
-      xs >= 0 && xs + kSweepCols <= a.W && y0 - 2 * K >= 0 && y0 + R + 2 * K <= a.H;
-  if (interior)
-    sweep_unit<K, F16, true, P>(a, b, d, f, ring, xs, y0, R, mask);
-  else
-    sweep_unit<K, F16, false, P>(a, b, d, f, ring, xs, y0, R, mask);
 }
 
 template <int K, int P>
@@ -405,17 +479,37 @@ cudaError_t launch_sweep_step(int k, int rows, int ring, int flux_storage, const
     case 4: fn = sweep_fn<4, 4>(flux_storage); break;
     default: return cudaErrorInvalidValue;
   }
-  if (rows < 1) return cudaErrorInvalidValue;
+  if (rows < 1 || !a.queue) return cudaErrorInvalidValue;
   const int valid = kSweepCols - 4 * k;
   const long long strips = (a.W + valid - 1) / valid, bands = (a.H + rows - 1) / rows;
-  const long long blocks = (strips * bands + kSweepWarps - 1) / kSweepWarps;
-  if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  const long long units = strips * bands;
+  if (units > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
   const size_t smem = sweep_smem_bytes(flux_storage, ring);
-  if (smem > 48 * 1024) {
-    const cudaError_t e =
-        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
+  // one wave of persistent CTAs (occupancy of this instantiation, queried once)
+  static std::mutex mu;
+  static std::map<const void*, int> resident;
+  int per_sm = 0, sms = 0;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = resident.find(fn);
+    if (it == resident.end()) {
+      cudaError_t e = cudaSuccess;
+      if (smem > 48 * 1024)
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      int n = 0;
+      if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kSweepThreads, smem);
+      if (e != cudaSuccess) return e;
+      it = resident.emplace(fn, n > 0 ? n : 1).first;
+    }
+    per_sm = it->second;
   }
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
+    sms = 1;
+  const long long blocks =
+      std::min<long long>((units + kSweepWarps - 1) / kSweepWarps, (long long)per_sm * sms);
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;

@@ -122,3 +122,27 @@ def test_sweep_full_size_4096(tws, oracle):
         assert_bitexact(gd, od, f"depth K={k}")
         assert_bitexact(gf, of, f"flux K={k}")
         assert_bitexact(gv, ov, f"flow map K={k}")
+
+
+def test_large_fp32_grid_default_is_bitexact(tws, oracle):
+    """A grid of at least 12 Mi cells with FP32 flux and nothing pinned runs the
+    three-step sweep by default; 5 steps (one sweep launch and a two-step
+    remainder) give the oracle's bits."""
+    W, H = 3584, 3600
+    p = tws.params_physical(boundary=tws.BOUNDARY_CLOSED)
+    rain = tws.rain_disks(44, W, H, 40, 0.02, 2)
+    b, d = oracle.terrain(44, W, H, 40.0, 15.0)
+    f = np.zeros((H, W, 4), np.float32)
+    od, of, ov = oracle_run(oracle, b, d, f, p.as_tuple(), rain, 5, oracle.BOUNDARY_CLOSED)
+    with tws.Grid(W, H, p) as g:
+        g.generate_scene(44, 40.0, 15.0)
+        g.set_sources(rain)
+        n0 = tws.lib().tws_launch_count()
+        g.step(5)
+        g.sync()
+        launches = tws.lib().tws_launch_count() - n0
+        gd, gf, gv = g.download()
+    assert launches == 2  # a three-step and a two-step launch
+    assert_bitexact(gd, od, "depth")
+    assert_bitexact(gf, of, "flux")
+    assert_bitexact(gv, ov, "flow map")

@@ -1046,6 +1046,7 @@ struct tws_batch {
   std::vector<Graph> graphs;
   uint64_t chains = 0, graph_launches = 0;
   int* d_err = nullptr;  // one device error word for every member while batched
+  int uploaded_variant = -1;  // variant whose unit table the device holds
   int h_err = 0;
   std::string last_error;
 };
@@ -1193,7 +1194,7 @@ int run_chain(tws_batch* b, int variant, const std::vector<int>& launches) {
     ++m;
   }
   if (m == 0) return TWS_OK;
-  const int blocks = launch_blocks(units);
+  const int blocks = launch_blocks(units);  // a power of two, so graphs stay reusable
   rc = ensure_units(b, blocks);
   if (rc != TWS_OK) return rc;
   // wait until the copy that last read this staging slot has completed
@@ -1208,10 +1209,10 @@ int run_chain(tws_batch* b, int variant, const std::vector<int>& launches) {
   for (int i = 0; i < n; ++i) {
     if (launches[i] <= 0) continue;
     tws_grid* g = b->grids[i];
-    VariantMaps* maps = maps_for(g, sv, &why);
-    if (!maps) return bfail(b, TWS_ERR_CUDA, why);
     BatchGrid& e = hg[m];
     std::memset(&e, 0, sizeof(e));  // padding too, so equal tables compare equal
+    VariantMaps* maps = maps_for(g, sv, &why);
+    if (!maps) return bfail(b, TWS_ERR_CUDA, why);
     if (!maps->on_device) {
       // written once per (grid, variant); the first chain's CTAs fence them
       CUtensorMap five[5] = {maps->b, maps->d[0], maps->d[1], maps->f[0], maps->f[1]};
@@ -1245,6 +1246,7 @@ int run_chain(tws_batch* b, int variant, const std::vector<int>& launches) {
   // members and the launch size.
   const int prev = b->uploaded_slot;
   const bool same = prev >= 0 && b->uploaded_m == m && b->uploaded_blocks == blocks &&
+                    b->uploaded_variant == variant &&
                     std::memcmp(hg, b->h_grids[prev], sizeof(BatchGrid) * m) == 0;
   if (same) {
     b->slot = prev ^ 1;  // keep the uploaded copy in its slot for the next comparison
@@ -1261,6 +1263,7 @@ int run_chain(tws_batch* b, int variant, const std::vector<int>& launches) {
     b->uploaded_slot = s;
     b->uploaded_m = m;
     b->uploaded_blocks = blocks;
+    b->uploaded_variant = variant;
   }
   cudaGraphExec_t exec = b->use_graphs ? graph_for(b, variant, max_l, blocks) : nullptr;
   if (exec) {

@@ -55,10 +55,15 @@ __device__ __forceinline__ float quantize_f16(float v, float scale, float inv_sc
   const float s = fminf(fmul(v, scale), 65504.0f);
   return fmul(__half2float(__float2half_rn(s)), inv_scale);
 }
+// The pair form: one saturating conversion (cvt.rn.satfinite.f16x2.f32) in
+// place of min(s, 65504) and a round-to-nearest conversion.  The two agree for
+// every input but NaN, which an outflow never is: values of 65520 and above,
+// which round to infinity, saturate to 65504 as the clamp gives.
 __device__ __forceinline__ float2 quantize_f16x2(float2 v, float2 scale, float2 inv_scale) {
   const float2 s = fmul2(v, scale);
-  const __half2 h = __floats2half2_rn(fminf(s.x, 65504.0f), fminf(s.y, 65504.0f));
-  return fmul2(__half22float2(h), inv_scale);
+  uint32_t packed;
+  asm("cvt.rn.satfinite.f16x2.f32 %0, %1, %2;" : "=r"(packed) : "f"(s.y), "f"(s.x));
+  return fmul2(__half22float2(*reinterpret_cast<const __half2*>(&packed)), inv_scale);
 }
 
 // GLSL clamp(v, 0, 1).

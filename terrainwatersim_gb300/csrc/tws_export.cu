@@ -260,9 +260,10 @@ __device__ __forceinline__ float avg4(float a, float b, float c, float d) {
   return fmul(fadd(fadd(a, b), fadd(c, d)), 0.25f);
 }
 
-// Up to kMipChain levels of the mip pyramid in one launch.  A CTA loads a
-// 32 x 32 texel block of the source level into shared memory and halves it
-// level by level with the 2 x 2 filter ((a + b) + (c + e)) * 0.25 (a, b the
+// Up to kMipChain levels of the mip pyramid in one launch.  A CTA takes a
+// 32 x 32 texel block of the source level: each thread filters a 2 x 2 quad
+// of it into the first level in registers, and the CTA halves that in shared
+// memory level by level with the 2 x 2 filter ((a + b) + (c + e)) * 0.25 (a, b the
 // upper texel pair, c, e the lower), writing each level's texels of
 // the block.  Level l + m texel q depends only on source texels
 // [q 2^m, (q + 1) 2^m), so every texel of a level of floor(w / 2^m) texels
@@ -278,19 +279,33 @@ struct MipChain {
 
 __global__ void __launch_bounds__(256)
     mip_chain_kernel(const float4* __restrict__ src, int sw, int sh, MipChain c) {
-  __shared__ float4 buf[2][kMipBlock * kMipBlock];
+  constexpr int Q = kMipBlock / 2;  // the first level's texels per block side
+  __shared__ float4 buf[2][Q * Q];
   const int bx = blockIdx.x * kMipBlock, by = blockIdx.y * kMipBlock;
   const int tid = threadIdx.x;
-  for (int i = tid; i < kMipBlock * kMipBlock; i += blockDim.x) {
-    const int x = bx + (i % kMipBlock), y = by + (i / kMipBlock);
-    buf[0][i] = (x < sw && y < sh) ? src[(size_t)y * sw + x] : make_float4(0.f, 0.f, 0.f, 0.f);
+  {
+    // the first level: each thread filters its 2 x 2 source texels in
+    // registers (texels past the source's edge read as zero; the output they
+    // feed is past the level's edge and not written)
+    const int qx = tid % Q, qy = tid / Q;
+    const int x = bx + 2 * qx, y = by + 2 * qy;
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    auto at = [&](int xx, int yy) {
+      return (xx < sw && yy < sh) ? src[(size_t)yy * sw + xx] : z;
+    };
+    const float4 a = at(x, y), b = at(x + 1, y), cc = at(x, y + 1), e = at(x + 1, y + 1);
+    const float4 r = make_float4(avg4(a.x, b.x, cc.x, e.x), avg4(a.y, b.y, cc.y, e.y),
+                                 avg4(a.z, b.z, cc.z, e.z), avg4(a.w, b.w, cc.w, e.w));
+    buf[0][qy * Q + qx] = r;
+    const int gx = (bx >> 1) + qx, gy = (by >> 1) + qy;
+    if (gx < c.w[0] && gy < c.h[0]) c.dst[0][(size_t)gy * c.w[0] + gx] = r;
   }
   __syncthreads();
-  int side = kMipBlock;
-  for (int l = 0; l < c.n; ++l) {
+  int side = Q;
+  for (int l = 1; l < c.n; ++l) {
     const int half = side / 2;
-    const float4* in = buf[l & 1];
-    float4* out = buf[(l + 1) & 1];
+    const float4* in = buf[(l - 1) & 1];
+    float4* out = buf[l & 1];
     const int ox = bx >> (l + 1), oy = by >> (l + 1);  // the block's origin in this level
     for (int i = tid; i < half * half; i += blockDim.x) {
       const int x = i % half, y = i / half;

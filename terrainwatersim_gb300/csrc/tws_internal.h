@@ -122,6 +122,7 @@ cudaError_t launch_step(int variant, int flux_storage, const CUtensorMap* tm_b,
 // ring of `ring` rows per lane (4)
 cudaError_t launch_sweep_step(int k, int rows, int ring, int flux_storage, const float* b,
                               const float* d, const void* f, const StepArgs& a, cudaStream_t s);
+constexpr int kSweepCtaThreads = 128;  // four warps, each its own sweep
 size_t sweep_smem_bytes(int flux_storage, int ring);
 int sweep_valid_columns(int k);
 // tws_stream.cu

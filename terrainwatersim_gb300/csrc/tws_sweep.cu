@@ -46,8 +46,8 @@
 namespace tws {
 namespace {
 
-constexpr int kSweepWarps = 4;
-constexpr int kSweepThreads = 32 * kSweepWarps;
+constexpr int kSweepThreads = kSweepCtaThreads;
+constexpr int kSweepWarps = kSweepThreads / 32;
 constexpr int kSweepCols = 64;  // columns a warp loads
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
@@ -104,7 +104,9 @@ struct SweepRing {
 template <int K, bool F16, bool INTERIOR, int P>
 __device__ __forceinline__ void sweep_unit(const StepArgs& a, const float* __restrict__ gb,
                                            const float* __restrict__ gd,
-                                           const void* __restrict__ gf, unsigned char* ring,
+                                           const void* __restrict__ gf,
+                                           float* __restrict__ d_out, void* __restrict__ f_out,
+                                           float2* __restrict__ v_out, unsigned char* ring,
                                            int xs, int y0, int R, uint32_t mask) {
   using RG = SweepRing<F16, P>;
   constexpr int HALO = 2 * K;
@@ -328,8 +330,8 @@ __device__ __forceinline__ void sweep_unit(const StepArgs& a, const float* __res
         const float2 vx = fsub2(fsub2(X1, own.x), fsub2(X0, own.y));
         const float2 vy = fsub2(fsub2(Y1, own.z), fsub2(Y0, own.w));
         if (INTERIOR || in1) {
-          *reinterpret_cast<float2*>(a.d_out + g) = dn;
-          *reinterpret_cast<float4*>(a.v_out + g) = make_float4(vx.x, vy.x, vx.y, vy.y);
+          *reinterpret_cast<float2*>(d_out + g) = dn;
+          *reinterpret_cast<float4*>(v_out + g) = make_float4(vx.x, vy.x, vx.y, vy.y);
           if constexpr (F16) {
             const __half2 p0 = __float22half2_rn(fmul2(make_float2(own.x.x, own.y.x), fscale2));
             const __half2 q0 = __float22half2_rn(fmul2(make_float2(own.z.x, own.w.x), fscale2));
@@ -340,24 +342,24 @@ __device__ __forceinline__ void sweep_unit(const StepArgs& a, const float* __res
             packed.y = *reinterpret_cast<const uint32_t*>(&q0);
             packed.z = *reinterpret_cast<const uint32_t*>(&p1);
             packed.w = *reinterpret_cast<const uint32_t*>(&q1);
-            *reinterpret_cast<uint4*>(reinterpret_cast<uint2*>(a.f_out) + g) = packed;
+            *reinterpret_cast<uint4*>(reinterpret_cast<uint2*>(f_out) + g) = packed;
           } else {
-            float4* fo = reinterpret_cast<float4*>(a.f_out) + g;
+            float4* fo = reinterpret_cast<float4*>(f_out) + g;
             fo[0] = make_float4(own.x.x, own.y.x, own.z.x, own.w.x);
             fo[1] = make_float4(own.x.y, own.y.y, own.z.y, own.w.y);
           }
         } else if (in0) {  // the grid's last column (odd width)
-          a.d_out[g] = dn.x;
-          a.v_out[g] = make_float2(vx.x, vy.x);
+          d_out[g] = dn.x;
+          v_out[g] = make_float2(vx.x, vy.x);
           if constexpr (F16) {
             const __half2 p0 = __float22half2_rn(fmul2(make_float2(own.x.x, own.y.x), fscale2));
             const __half2 q0 = __float22half2_rn(fmul2(make_float2(own.z.x, own.w.x), fscale2));
             uint2 packed;
             packed.x = *reinterpret_cast<const uint32_t*>(&p0);
             packed.y = *reinterpret_cast<const uint32_t*>(&q0);
-            reinterpret_cast<uint2*>(a.f_out)[g] = packed;
+            reinterpret_cast<uint2*>(f_out)[g] = packed;
           } else {
-            reinterpret_cast<float4*>(a.f_out)[g] =
+            reinterpret_cast<float4*>(f_out)[g] =
                 make_float4(own.x.x, own.y.x, own.z.x, own.w.x);
           }
         }
@@ -437,9 +439,9 @@ __global__ void __launch_bounds__(kSweepThreads, (K <= 2 ? 4 : (K == 3 ? 3 : 2))
     const bool interior =
         xs >= 0 && xs + kSweepCols <= a.W && y0 - 2 * K >= 0 && y0 + R + 2 * K <= a.H;
     if (interior)
-      sweep_unit<K, F16, true, P>(a, b, d, f, ring, xs, y0, R, mask);
+      sweep_unit<K, F16, true, P>(a, b, d, f, a.d_out, a.f_out, a.v_out, ring, xs, y0, R, mask);
     else
-      sweep_unit<K, F16, false, P>(a, b, d, f, ring, xs, y0, R, mask);
+      sweep_unit<K, F16, false, P>(a, b, d, f, a.d_out, a.f_out, a.v_out, ring, xs, y0, R, mask);
   }
   // The last warp to finish resets the queue for the next launch: every other
   // warp has made its final claim by then, and the next launch reads the

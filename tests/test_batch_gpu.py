@@ -112,9 +112,12 @@ def test_batch_step_each_and_join_leave(tws, oracle, graphs):
         g.close()
 
 
-def test_batch_fp16_storage_matches_oracle(tws, oracle):
-    made = [make_grid(tws, oracle, s, flux_storage=tws.FLUX_F16) for s in SPECS[:4]]
+@pytest.mark.parametrize("variant", [None, 1, 6])
+def test_batch_fp16_storage_matches_oracle(tws, oracle, variant):
+    made = [make_grid(tws, oracle, s, flux_storage=tws.FLUX_F16) for s in SPECS[:4] + SPECS[6:]]
     with tws.Batch(tws.FLUX_F16) as batch:
+        if variant is not None:
+            batch.set_variant(variant)
         for g, _ in made:
             batch.add(g)
         batch.step(24)
@@ -230,5 +233,35 @@ def test_batch_autotune_preserves_state(tws, oracle):
             gd, gf, gv = g.download()
             assert_bitexact(gd, od, "depth")
             assert_bitexact(gf, of, "flux")
+    for g, _ in made:
+        g.close()
+
+
+@pytest.mark.parametrize("variant", [4, 6])
+def test_batch_uneven_steps_and_membership(tws, oracle, variant):
+    """Members with different step counts (remainders that are not multiples
+    of K run as one-step launches), a member joining between calls and one
+    leaving, every result bit-exact."""
+    made = [make_grid(tws, oracle, s) for s in SPECS]
+    counts = [5, 17, 0, 33, 2, 11, 40]
+    with tws.Batch() as batch:
+        batch.set_variant(variant)
+        for g, _ in made[:-1]:
+            batch.add(g)
+        batch.step_each(counts[:-1])
+        batch.sync()
+        batch.add(made[-1][0])  # joins
+        batch.remove(made[0][0])  # leaves
+        batch.step_each([4] * (len(made) - 1))
+        batch.sync()
+        for i, (g, setup) in enumerate(made):
+            total = counts[i] + (4 if i > 0 else 0)
+            if i == len(made) - 1:
+                total = 4
+            od, of, ov = oracle_state(oracle, setup, total)
+            gd, gf, gv = g.download()
+            assert_bitexact(gd, od, f"depth {g.width}x{g.height}")
+            assert_bitexact(gf, of, f"flux {g.width}x{g.height}")
+            assert_bitexact(gv, ov, f"velocity {g.width}x{g.height}")
     for g, _ in made:
         g.close()

@@ -129,5 +129,29 @@ static __device__ __noinline__ float add_sources(float d, int gx, int gy, const 
   return d;
 }
 
+// The sources of `mask` at cell (gx, gy), in source order as add_sources
+// applies them, without a call: for the compact source passes of the step
+// kernels, where one call per cell sat on a launch's critical path (the warps
+// under a rain disk were the slowest of a launch) and the saved registers
+// around a call would cost the unrolled code around it.
+__device__ __forceinline__ float add_sources_inline(float d, int gx, int gy, const StepArgs& a,
+                                                    uint32_t mask) {
+#pragma unroll 1
+  for (int k = 0; k < a.nsrc; ++k) {
+    if (!((mask >> k) & 1u)) continue;
+    const DevSource& s = a.src[k];
+    if (gx < s.bx0 || gx > s.bx1 || gy < s.by0 || gy > s.by1) continue;
+    if (s.kind == TWS_SOURCE_DISK) {
+      const long long dx = gx - s.icx, dy = gy - s.icy;
+      if (dx * dx + dy * dy <= (long long)s.ir * s.ir) d = add_rain(d, s.rate, gx, gy);
+    } else {
+      const float tx = fsub(s.cx, (float)gx), ty = fsub(s.cy, (float)gy);
+      const float q = fdiv(fadd(fmul(tx, tx), fmul(ty, ty)), s.radius);
+      const float inc = fmul(saturate01(fsub(1.0f, q)), s.rate);
+      if (inc != 0.0f) d = fadd(d, inc);
+    }
+  }
+  return d;
+}
 
 }  // namespace tws

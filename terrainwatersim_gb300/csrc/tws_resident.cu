@@ -198,7 +198,7 @@ __global__ void __launch_bounds__(kResThreads, 1)
   }
   auto sources = [&](float d, int x, int y) {
     if (mask != 0u && x >= ux0 && x <= ux1 && y >= uy0 && y <= uy1)
-      d = add_sources(d, x, y, a, mask);
+      d = add_sources_inline(d, x, y, a, mask);
     return d;
   };
 

@@ -226,20 +226,18 @@ __device__ __forceinline__ void process_tile(const StepArgs& a, float* __restric
   const bool closed = a.closed != 0;
 
   // Phase 0: first step's sources, surface height h = d + b (flowUpdate.comp:34).
+  // The sources are a compact pass of their own (only tiles a source reaches
+  // make it), with the same cells per thread as the loop after it.
   if (mask) {
+#pragma unroll 1
     for (int idx = tid; idx < T::NB; idx += kThreads) {
-      float d = sd[idx];
       const int i = idx / T::BW, j = idx - (idx / T::BW) * T::BW;
       const int gx = x0 - T::HX + j, gy = y0 - T::HY + i;
-      if (INTERIOR || (gx >= 0 && gx < W && gy >= 0 && gy < H)) {
-        d = add_sources(d, gx, gy, a, mask);
-        sd[idx] = d;
-      }
-      sh[idx] = fadd(d, sb[idx]);
+      if (INTERIOR || (gx >= 0 && gx < W && gy >= 0 && gy < H))
+        sd[idx] = add_sources_inline(sd[idx], gx, gy, a, mask);
     }
-  } else {
-    for (int idx = tid; idx < T::NB; idx += kThreads) sh[idx] = fadd(sd[idx], sb[idx]);
   }
+  for (int idx = tid; idx < T::NB; idx += kThreads) sh[idx] = fadd(sd[idx], sb[idx]);
   if (F16) {
     const __half2* st = reinterpret_cast<const __half2*>(staging);
     for (int idx = tid; idx < T::NF; idx += kThreads) {
@@ -340,9 +338,22 @@ __device__ __forceinline__ void process_tile(const StepArgs& a, float* __restric
           v_out[g] = make_float2(fsub(fsub(X1, fc.x), fsub(X0, fc.y)),
                                    fsub(fsub(Y1, fc.z), fsub(Y0, fc.w)));
         } else {
-          const float dnext = mask ? add_sources(dn, gx, gy, a, mask) : dn;
-          sd[bidx] = dnext;
-          sh[bidx] = fadd(dnext, sb[bidx]);
+          sd[bidx] = dn;
+          sh[bidx] = fadd(dn, sb[bidx]);
+        }
+      }
+      if (s < K - 1 && mask) {
+        // the next step's sources: a compact pass over the same cells per thread
+#pragma unroll 1
+        for (int idx = tid; idx < RW * RH; idx += kThreads) {
+          const int i = idx / RW, j = idx - (idx / RW) * RW;
+          const int fi = T::RF - rd + i, fj = T::RF - rd + j;
+          const int gx = x0 - T::RF + fj, gy = y0 - T::RF + fi;
+          if (!INTERIOR && (gx < 0 || gx >= W || gy < 0 || gy >= H)) continue;
+          const int bidx = (fi + T::HY - T::RF) * T::BW + (fj + T::HX - T::RF);
+          const float d = add_sources_inline(sd[bidx], gx, gy, a, mask);
+          sd[bidx] = d;
+          sh[bidx] = fadd(d, sb[bidx]);
         }
       }
     }
@@ -427,20 +438,17 @@ __device__ __forceinline__ void process_tile_flat(const StepArgs& a, float* __re
   constexpr auto first = [](int r) { return (T::HY - r) * S + (T::HX - r); };
   constexpr auto last = [](int r) { return (T::HY + TY + r - 1) * S + (T::HX + TX + r - 1); };
 
-  // Phase 0: first step's sources and h = d + b (flowUpdate.comp:34).
+  // Phase 0: first step's sources and h = d + b (flowUpdate.comp:34).  The
+  // sources are a compact pass of their own, outside the unrolled runs (only
+  // tiles a source reaches make it), over the same cells per thread as the
+  // run after it.
   if (mask) {
-    ring_for<0, T::NB - 1, INTERIOR>(tid, [&](int p) {
+    ring_for<0, T::NB - 1, false>(tid, [&](int p) {
       int gx, gy;
-      float d = sd[p];
-      if (cell(p, gx, gy)) {
-        d = add_sources(d, gx, gy, a, mask);
-        sd[p] = d;
-      }
-      sh[p] = fadd(d, sb[p]);
+      if (cell(p, gx, gy)) sd[p] = add_sources_inline(sd[p], gx, gy, a, mask);
     });
-  } else {
-    ring_for<0, T::NB - 1, INTERIOR>(tid, [&](int p) { sh[p] = fadd(sd[p], sb[p]); });
   }
+  ring_for<0, T::NB - 1, INTERIOR>(tid, [&](int p) { sh[p] = fadd(sd[p], sb[p]); });
   // The flux of cell p as the TMA box holds it (float4 records, or halves).
   auto box_flux = [&](int p) -> float4 {
     if constexpr (F16) {
@@ -526,19 +534,25 @@ __device__ __forceinline__ void process_tile_flat(const StepArgs& a, float* __re
     io = fadd2(io, make_float2(fw[p + S], fc.z));
     return fadd2(io, make_float2(fz[p - S], fc.w));
   };
-  // Phase B: depth update, flowApply.comp:32-52, then the next step's sources
-  // and surface height.
+  // Phase B: depth update, flowApply.comp:32-52, and surface height; the next
+  // step's sources follow in their own pass (depth_sources).
   auto depth = [&](int p) {
-    int gx = 0, gy = 0;
-    if (!INTERIOR || mask) {
+    if constexpr (!INTERIOR) {
+      int gx, gy;
       if (!cell(p, gx, gy)) return;  // off the grid: depth and surface stay zero
     }
     const float4 fc = make_float4(fx[p], fy[p], fz[p], fw[p]);
     const float2 io = in_out(p, fc);
-    float dn = max0_fast(fadd(sd[p], fmul(fsub(io.x, io.y), cc)));
-    if (mask) dn = add_sources(dn, gx, gy, a, mask);
+    const float dn = max0_fast(fadd(sd[p], fmul(fsub(io.x, io.y), cc)));
     sd[p] = dn;
     sh[p] = fadd(dn, sb[p]);
+  };
+  auto depth_sources = [&](int p) {
+    int gx, gy;
+    if (!cell(p, gx, gy)) return;
+    const float d = add_sources_inline(sd[p], gx, gy, a, mask);
+    sd[p] = d;
+    sh[p] = fadd(d, sb[p]);
   };
   // The last step's depth ring is the tile itself: depth, flux and flow map
   // (flowApply.comp:32-52) go out to the grid.
@@ -597,6 +611,8 @@ __device__ __forceinline__ void process_tile_flat(const StepArgs& a, float* __re
     __syncthreads();
     if constexpr (s < K - 1) {
       ring_for<first(rf - 1), last(rf - 1), INTERIOR>(tid, depth);
+      // same cells per thread as the run above: no barrier between the two
+      if (mask) ring_for<first(rf - 1), last(rf - 1), false>(tid, depth_sources);
       __syncthreads();
     } else {
       finish();

@@ -91,7 +91,7 @@ __device__ __forceinline__ void stream_unit(const StepArgs& a, const float* __re
   const bool out_lane = lane >= 1 && lane <= kStrip && (INTERIOR || gx < W);
 
   auto with_sources = [&](float dv, int x, int r, bool in) -> float {
-    return (mask && in && r >= 0 && r < H) ? add_sources(dv, x, r, a, mask) : dv;
+    return (mask && in && r >= 0 && r < H) ? add_sources_inline(dv, x, r, a, mask) : dv;
   };
 
   // Window: rows r-1, r, r+1 of h; d of rows r-1, r; new outflow of r-1, r.

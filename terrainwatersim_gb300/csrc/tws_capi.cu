@@ -1110,9 +1110,13 @@ int ensure_capacity(tws_batch* b, int n) {
   return TWS_OK;
 }
 
-// Grow the unit table to n entries (n is a launch's CTA count, a power of two).
+// Grow the unit table to at least n entries (a launch's CTA count), in powers
+// of two so that a changing membership rarely reallocates it.
 int ensure_units(tws_batch* b, int n) {
   if (n <= b->ucap) return TWS_OK;
+  int cap = 256;
+  while (cap < n) cap *= 2;
+  n = cap;
   cudaStreamSynchronize(b->stream);
   drop_graphs(b);
   free_units(b);
@@ -1141,12 +1145,17 @@ int run_launches(tws_batch* b, int variant, int launches, int blocks) {
   return TWS_OK;
 }
 
-// CTAs per launch for a chain of `units` tiles: the next power of two (at
-// least 256), so that graphs stay reusable while the membership changes.
+// CTAs per launch for a chain of `units` tiles: the next of 256, 288, ...,
+// 480, 512, 576, ... (eight sizes per doubling), so that graphs stay reusable
+// while the membership changes and at most an eighth of the CTAs launch only
+// to return (a power of two wasted up to half: 2,496 of 8,192 on the 64-grid
+// configuration).
 int launch_blocks(int units) {
-  int n = 256;
-  while (n < units) n *= 2;
-  return n;
+  int p = 256;
+  while (2 * p <= units) p *= 2;  // p <= units < 2p (or units < 256)
+  if (units <= p) return p;
+  const int step = p / 8;
+  return (units + step - 1) / step * step;
 }
 
 cudaGraphExec_t graph_for(tws_batch* b, int variant, int launches, int blocks) {

@@ -1243,10 +1243,29 @@ int run_chain(tws_batch* b, int variant, const std::vector<int>& launches) {
     e.v = g->v;
     e.cur = g->cur;
     e.launches = launches[i];
-    const int meta = launches[i] | (g->cur << 30);
-    for (int y0 = 0; y0 < g->H; y0 += ty)
-      for (int x0 = 0; x0 < g->W; x0 += tx) hu[u++] = BatchUnit{m, x0, y0, meta};
     ++m;
+  }
+  // The units: every member's interior tiles first, then the tiles at the
+  // members' edges, so that the CTAs resident on an SM at a time mostly run
+  // one of the two code paths (the edge path is separate code, and mixing
+  // the two stalled the schedulers on instruction fetch).  Interior is the
+  // kernel's test: the tile's b/d box (halo 2K rounded up to 4 in x, 2K in y)
+  // lies inside the grid.
+  const int hx = (2 * k + 3) / 4 * 4, hy = 2 * k;
+  for (int pass = 0; pass < 2; ++pass) {
+    m = 0;
+    for (int i = 0; i < n; ++i) {
+      if (launches[i] <= 0) continue;
+      const tws_grid* g = b->grids[i];
+      const int meta = launches[i] | (g->cur << 30);
+      for (int y0 = 0; y0 < g->H; y0 += ty)
+        for (int x0 = 0; x0 < g->W; x0 += tx) {
+          const bool interior = x0 - hx >= 0 && y0 - hy >= 0 && x0 + tx + hx <= g->W &&
+                                y0 + ty + hy <= g->H;
+          if (interior == (pass == 0)) hu[u++] = BatchUnit{m, x0, y0, meta};
+        }
+      ++m;
+    }
   }
   for (; u < blocks; ++u) hu[u] = BatchUnit{0, 0, 0, 0};  // CTAs past the units return
   // Upload the table unless it equals the one the device already holds (the

@@ -223,20 +223,27 @@ def aggregate_gcell_steps(cells: int, sim_steps: int, world_size: int, seconds: 
 
 # ------------------------------------------------------------------ our arm
 
-def variant_form(v):
+def variant_form(v, tail=0):
     """How a variant runs: one CTA per tile, persistent CTAs, register
-    streaming, or a row sweep (with its rows per loop trip)."""
+    streaming, or a row sweep (with its rows per loop trip and the height of
+    the short bands that end its queue)."""
     kind = v[5] if len(v) > 5 else 0
     if kind == 1:
         return "stream"
     if kind == 2:
-        return f"sweep_u{v[3]}"
+        return f"sweep_u{v[3]}" + (f"_tail{tail}" if tail else "")
     return "persistent" if v[3] > 1 else "pertile"
 
 
 def kernel_name(v):
     kind = v[5] if len(v) > 5 else 0
     return {1: "stream_kernel", 2: "sweep_kernel"}.get(kind, "step_kernel")
+
+
+def kernel_label(v, tail=0):
+    """e.g. sweep_kernel<K=3,52x256,tail 64> or step_kernel<K=2,32x32>."""
+    return (f"{kernel_name(v)}<K={v[0]},{v[1]}x{v[2]}" + (f",tail {tail}" if tail else "")
+            + ">")
 
 
 def scene(tws, size):
@@ -288,6 +295,7 @@ def run_ours(args):
 
     # every kernel variant (plain and temporally blocked, several tiles), same workload
     vinfo = tws.variants()
+    tails = [tws.variant_tail_rows(i) for i in range(len(vinfo))]
     variants = {}
     if not args.no_sweep:
         sweep_steps = max(3, steps // 5)
@@ -435,11 +443,11 @@ def run_ours(args):
                 "launch_us": round(launch_s * 1e6, 2),
                 "traffic": round(tpc * cells, 0) if tpc else None,
                 "dram_gbs": round(tpc * cells / launch_s / 1e9, 1) if tpc else None,
-                "kernel": f"{kernel_name(vinfo[best_v])}<K={best_k},"
-                          f"{vinfo[best_v][1]}x{vinfo[best_v][2]}>",
+                "kernel": kernel_label(vinfo[best_v], tails[best_v]),
             },
             "roofline_by_kernel": {
-                (f"{i}_{kernel_name(vinfo[i])}_k{vinfo[i][0]}_{vinfo[i][1]}x{vinfo[i][2]}"): {
+                (f"{i}_{kernel_name(vinfo[i])}_k{vinfo[i][0]}_{vinfo[i][1]}x{vinfo[i][2]}"
+                 + (f"_tail{tails[i]}" if tails[i] else "")): {
                     "launch_us": round(v["seconds"] / max(1, v["launches"]) * 1e6, 2),
                     "frac": round(bpc * cells / (v["seconds"] / max(1, v["launches"])) / 1e9
                                   / peak, 4),
@@ -451,7 +459,7 @@ def run_ours(args):
                              "latency, not HBM: profiles/sweep_kernel_k3_40rows_4096.md)",
             "variants": {
                 (f"{i}_{'plain' if vinfo[i][0] == 1 else 'blocked_k%d' % vinfo[i][0]}"
-                 f"_{vinfo[i][1]}x{vinfo[i][2]}_{variant_form(vinfo[i])}"): {
+                 f"_{vinfo[i][1]}x{vinfo[i][2]}_{variant_form(vinfo[i], tails[i])}"): {
                     "variant": i,
                     "gcell_steps_per_s": round(cells * chain * v["steps"] * ws / v["seconds"] / 1e9,
                                                3),

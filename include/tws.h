@@ -199,6 +199,11 @@ TWS_API int tws_variant_info(int variant, int* steps_per_launch, int* tile_x, in
 #define TWS_VARIANT_STREAM 1
 #define TWS_VARIANT_SWEEP 2
 TWS_API int tws_variant_kind(int variant);
+/* Rows of the short bands that end a sweep variant's work queue (its other
+ * bands are tile_y rows; the short ones are the grid's last rows, about one
+ * unit per resident warp), 0 for none and for other kinds, or
+ * TWS_ERR_INVALID past the last variant. */
+TWS_API int tws_variant_tail_rows(int variant);
 
 /* Pin a variant for this grid (-1: automatic -- the tuned choice for this
  * grid shape if tws_autotune ran for one, else the steps-per-launch setting). */

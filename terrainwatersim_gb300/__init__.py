@@ -110,6 +110,7 @@ def _declare(L):
         "tws_variant_count": ([], i),
         "tws_variant_info": ([i, vp, vp, vp, vp, vp], i),
         "tws_variant_kind": ([i], i),
+        "tws_variant_tail_rows": ([i], i),
         "tws_set_variant": ([vp, i], i),
         "tws_set_wait_limit": ([vp, C.c_longlong], i),
         "tws_test_drop_tile_loads": ([vp, i], i),
@@ -226,6 +227,14 @@ def variants():
         _check(min(kind, 0))
         out.append((k.value, tx.value, ty.value, st.value, sm.value, kind))
     return out
+
+
+def variant_tail_rows(variant: int) -> int:
+    """Rows of the short bands that end a sweep variant's work queue (0: all
+    bands are tile_y rows)."""
+    r = lib().tws_variant_tail_rows(variant)
+    _check(min(r, 0))
+    return int(r)
 
 
 def resident_fits(width: int, height: int, flux_storage: int = FLUX_F32) -> int:

@@ -186,7 +186,7 @@ int chosen_variant(const tws_grid* g) {
     if (t.variant >= 0) return t.variant;
   }
   if (g->steps_per_launch == 0 && (long long)g->W * g->H >= kLargeGridCells) {
-    const int v = step_variant_large_grid(g->flux_storage);
+    const int v = step_variant_large_grid(g->flux_storage, g->W, g->H);
     if (v >= 0) return v;
   }
   const int k = g->steps_per_launch > 0 ? g->steps_per_launch : default_steps_per_launch(g);
@@ -597,6 +597,11 @@ TWS_API int tws_variant_info(int i, int* k, int* tx, int* ty, int* stages, size_
   if (stages) *stages = v.stages;
   if (smem) *smem = v.smem;
   return TWS_OK;
+}
+
+TWS_API int tws_variant_tail_rows(int i) {
+  if (i < 0 || i >= step_variant_count()) return TWS_ERR_INVALID;
+  return step_variant(i).kind == kKindSweep ? step_variant(i).ry_tail : 0;
 }
 
 TWS_API int tws_variant_kind(int i) {

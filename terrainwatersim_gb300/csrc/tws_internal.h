@@ -55,6 +55,7 @@ struct StepVariant {
   int sw;     // F16 staging width in cells (whole pairs)
   int uni;    // unified layout: the flux box is the b/d box
   int ring;   // kKindSweep: rows in each lane's load ring
+  int ry_tail; // kKindSweep: rows of the short bands that end the work queue (0: none)
   size_t smem;
 };
 
@@ -110,17 +111,21 @@ constexpr long long kDefaultWaitCycles = 4000000000LL;
 int step_variant_count();
 const StepVariant& step_variant(int i);
 int step_variant_for(int k, int flux_storage);
-// The automatic choice for grids of at least kLargeGridCells cells, or -1.
+// The automatic choice for grids of at least kLargeGridCells cells (FP16
+// flux: kLargeF16Cells), or -1.
 constexpr long long kLargeGridCells = 12LL << 20;
-int step_variant_large_grid(int flux_storage);
+constexpr long long kLargeF16Cells = 48LL << 20;
+int step_variant_large_grid(int flux_storage, int W, int H);
 // Tile variants read through the tensor maps, stream variants through the
 // raw pointers (b, d, f of the current state).
 cudaError_t launch_step(int variant, int flux_storage, const CUtensorMap* tm_b,
                         const CUtensorMap* tm_d, const CUtensorMap* tm_f, const float* b,
                         const float* d, const void* f, const StepArgs& a, cudaStream_t s);
-// tws_sweep.cu: K = 2..4 steps per launch, `rows` rows per warp band, a
-// ring of `ring` rows per lane (4)
-cudaError_t launch_sweep_step(int k, int rows, int ring, int flux_storage, const float* b,
+// tws_sweep.cu: K = 2..4 steps per launch, `rows` rows per warp band (the
+// last bands `tail_rows` rows when it is above 0), a ring of `ring` rows per
+// lane (4)
+cudaError_t launch_sweep_step(int k, int rows, int tail_rows, int ring, int flux_storage,
+                              const float* b,
                               const float* d, const void* f, const StepArgs& a, cudaStream_t s);
 constexpr int kSweepCtaThreads = 128;  // four warps, each its own sweep
 size_t sweep_smem_bytes(int flux_storage, int ring);

@@ -865,7 +865,7 @@ VariantEntry make_entry() {
 }
 
 struct VariantTable {
-  static constexpr int kMax = 40;
+  static constexpr int kMax = 48;
   VariantEntry e[kMax + 1];  // one spare slot: an entry past kMax is dropped, not written over n
   int n = 0;
   std::mutex mu;
@@ -909,9 +909,24 @@ struct VariantTable {
     add_sweep(3, 48, 4);   // 27
     add_sweep(3, 64, 4);   // 28
     add_sweep(4, 64, 4);   // 29
+    // Taller bands, the last ones short (the tail: about one short unit per
+    // resident warp ends the work queue).  Tall bands recompute fewer halo
+    // rows per output row, and the tail keeps the launch's end short.
+    // FP32, K = 3 (Gcell-steps/s): 6144^2 80/32 223.6 (40: 205.8); 8192^2
+    // 192/48 248.7; 12288^2 384/64 253.4; 16384^2 256/64 256.2, 384/64 253.6
+    // (64: 233.9).  FP16, K = 2: 8192^2 96/32 232.1; 12288^2 192/48 245.2;
+    // 16384^2 192/48 249.9 (48: 226.2).
+    add_sweep(3, 80, 4, 32);   // 30
+    add_sweep(3, 128, 4, 48);  // 31
+    add_sweep(3, 192, 4, 48);  // 32
+    add_sweep(3, 256, 4, 64);  // 33
+    add_sweep(3, 384, 4, 64);  // 34
+    add_sweep(2, 96, 4, 32);   // 35
+    add_sweep(2, 192, 4, 48);  // 36
   }
-  void add_sweep(int k, int rows, int ring) {
+  void add_sweep(int k, int rows, int ring, int tail_rows = 0) {
     VariantEntry s{};
+    s.v.ry_tail = tail_rows;
     s.v.k = k;
     s.v.tx = sweep_valid_columns(k);
     s.v.ty = rows;
@@ -969,19 +984,45 @@ EncodeTiledFn encode_fn(std::string* why) {
 int step_variant_count() { return table().n; }
 const StepVariant& step_variant(int i) { return table().e[i].v; }
 
-int step_variant_large_grid(int flux_storage) {
-  // FP32 flux on large grids: the three-step row sweep with 40-row bands
-  // (4096^2: 199.7 against 192.2 for the two-step tiles; with FP16 storage
-  // and on smaller grids the tiles are faster)
-  if (flux_storage != TWS_FLUX_F32) return -1;
-  static const int v = [] {
+int step_variant_large_grid(int flux_storage, int W, int H) {
+  // FP32 flux: the three-step row sweep (4096^2: 40-row bands, 196.8-199.7
+  // Gcell-steps/s against 192-193 for the two-step tiles).  FP16 flux: the
+  // two-step sweep from kLargeF16Cells on; below it the tiles are faster
+  // (4096^2: 203.1 against 191.0).  The band height is the tallest on a
+  // ladder that leaves enough units per resident warp for the work queue to
+  // balance: 3.5 for K = 3 (three CTAs of four warps per SM), 5 for K = 2
+  // (four CTAs per SM); the thresholds are measured on 4096^2 to 16384^2.
+  const long long cells = (long long)W * H;
+  if (cells < kLargeGridCells) return -1;
+  const bool f32 = flux_storage == TWS_FLUX_F32;
+  if (!f32 && cells < kLargeF16Cells) return -1;
+  const int k = f32 ? 3 : 2;
+  static const int kLadder3[][2] = {{40, 0}, {80, 32}, {128, 48}, {192, 48}, {256, 64}, {384, 64}};
+  static const int kLadder2[][2] = {{48, 0}, {96, 32}, {192, 48}};
+  const int(*ladder)[2] = f32 ? kLadder3 : kLadder2;
+  const int rungs = f32 ? 6 : 3;
+  const double per_warp = f32 ? 3.5 : 5.0;
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    sms = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && n > 0
+              ? n
+              : 1;
+  }
+  const double warps = (double)sms * (f32 ? 3 : 4) * (kSweepCtaThreads / 32);
+  const long long strips = (W + sweep_valid_columns(k) - 1) / sweep_valid_columns(k);
+  int pick = -1;
+  for (int r = 0; r < rungs; ++r) {
+    const long long units = strips * ((H + ladder[r][0] - 1) / ladder[r][0]);
+    if (r > 0 && units < per_warp * warps) break;
     for (int i = 0; i < step_variant_count(); ++i) {
       const StepVariant& e = step_variant(i);
-      if (e.kind == kKindSweep && e.k == 3 && e.ry == 40) return i;
+      if (e.kind == kKindSweep && e.k == k && e.ry == ladder[r][0] && e.ry_tail == ladder[r][1])
+        pick = i;
     }
-    return -1;
-  }();
-  return v;
+  }
+  return pick;
 }
 
 int step_variant_for(int k, int /*flux_storage*/) {
@@ -1063,7 +1104,7 @@ cudaError_t launch_step(int variant, int flux_storage, const CUtensorMap* tm_b,
   VariantEntry& e = t.e[variant];
   if (e.v.kind == kKindStream) return launch_stream_step(e.v.ry, fs, b, d, f, a, s);
   if (e.v.kind == kKindSweep)
-    return launch_sweep_step(e.v.k, e.v.ry, e.v.ring, fs, b, d, f, a, s);
+    return launch_sweep_step(e.v.k, e.v.ry, e.v.ry_tail, e.v.ring, fs, b, d, f, a, s);
   if (!tm_b || !tm_d || !tm_f) return cudaErrorInvalidValue;
   const void* fn = e.fn[fs];
   const size_t smem = e.smem[fs];

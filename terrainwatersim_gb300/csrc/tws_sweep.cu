@@ -398,18 +398,34 @@ __device__ __forceinline__ void sweep_unit_coords(int i, int S, int B, int& s, i
   }
 }
 
+// The bands of a launch: rows [0, tall_end) in bands of `tall` rows (the
+// last one may be shorter), then rows [tall_end, H) in bands of `tail` rows.
+// Short bands come last in the work queue, so that the launch ends on small
+// units; tall bands recompute fewer halo rows per output row.
+struct SweepBands {
+  int tall, tall_end, tall_count, tail, count;
+};
+
+// Band i of a partition with a tail: its first row and its height.
+__device__ __forceinline__ void sweep_band(const SweepBands& sb, int H, int i, int& y0, int& R) {
+  const bool tall = i < sb.tall_count;
+  y0 = tall ? i * sb.tall : sb.tall_end + (i - sb.tall_count) * sb.tail;
+  R = min(tall ? sb.tall : sb.tail, (tall ? sb.tall_end : H) - y0);
+}
+
 // Persistent warps (one wave): each takes units (strip, band) from the grid's
 // queue until none is left, so warps that drew cheap units take more of them.
-template <int K, bool F16, int P>
+template <int K, bool F16, int P, bool TAIL>
 __global__ void __launch_bounds__(kSweepThreads, (K <= 2 ? 4 : (K == 3 ? 3 : 2)))
     sweep_kernel(const float* __restrict__ b, const float* __restrict__ d,
-                 const void* __restrict__ f, const __grid_constant__ StepArgs a, int R) {
+                 const void* __restrict__ f, const __grid_constant__ StepArgs a,
+                 const SweepBands sb) {
   using RG = SweepRing<F16, P>;
   constexpr int VALID = kSweepCols - 4 * K;
   extern __shared__ __align__(128) unsigned char sweep_smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int strips = (a.W + VALID - 1) / VALID;
-  const int bands = (a.H + R - 1) / R;
+  const int bands = sb.count;
   const int total = strips * bands;
   // the previous launch on the stream has completed and its writes (the
   // state, and the queue it reset) are visible before any global access
@@ -425,7 +441,13 @@ __global__ void __launch_bounds__(kSweepThreads, (K <= 2 ? 4 : (K == 3 ? 3 : 2))
     int si, bi;
     sweep_unit_coords(u, strips, bands, si, bi);
     const int xs = si * VALID - 2 * K;
-    const int y0 = bi * R;
+    int y0, R;
+    if constexpr (TAIL) {
+      sweep_band(sb, a.H, bi, y0, R);
+    } else {  // uniform bands: the height stays a kernel parameter
+      y0 = bi * sb.tall;
+      R = sb.tall;
+    }
     uint32_t mask = 0;
 #pragma unroll
     for (int k = 0; k < TWS_MAX_SOURCES; ++k) {
@@ -457,9 +479,12 @@ __global__ void __launch_bounds__(kSweepThreads, (K <= 2 ? 4 : (K == 3 ? 3 : 2))
 }
 
 template <int K, int P>
-const void* sweep_fn(int flux_storage) {
-  return flux_storage == TWS_FLUX_F16 ? reinterpret_cast<const void*>(&sweep_kernel<K, true, P>)
-                                      : reinterpret_cast<const void*>(&sweep_kernel<K, false, P>);
+const void* sweep_fn(int flux_storage, bool tail) {
+  if (flux_storage == TWS_FLUX_F16)
+    return tail ? reinterpret_cast<const void*>(&sweep_kernel<K, true, P, true>)
+                : reinterpret_cast<const void*>(&sweep_kernel<K, true, P, false>);
+  return tail ? reinterpret_cast<const void*>(&sweep_kernel<K, false, P, true>)
+              : reinterpret_cast<const void*>(&sweep_kernel<K, false, P, false>);
 }
 
 }  // namespace
@@ -471,21 +496,18 @@ size_t sweep_smem_bytes(int flux_storage, int ring) {
                                                                     : SweepRing<false, 1>::ROW);
 }
 
-cudaError_t launch_sweep_step(int k, int rows, int ring, int flux_storage, const float* b,
-                              const float* d, const void* f, const StepArgs& a, cudaStream_t s) {
+cudaError_t launch_sweep_step(int k, int rows, int tail_rows, int ring, int flux_storage,
+                              const float* b, const float* d, const void* f, const StepArgs& a,
+                              cudaStream_t s) {
   const void* fn = nullptr;
   if (ring != 4) return cudaErrorInvalidValue;
   switch (k) {
-    case 2: fn = sweep_fn<2, 4>(flux_storage); break;
-    case 3: fn = sweep_fn<3, 4>(flux_storage); break;
-    case 4: fn = sweep_fn<4, 4>(flux_storage); break;
+    case 2: fn = sweep_fn<2, 4>(flux_storage, tail_rows > 0); break;
+    case 3: fn = sweep_fn<3, 4>(flux_storage, tail_rows > 0); break;
+    case 4: fn = sweep_fn<4, 4>(flux_storage, tail_rows > 0); break;
     default: return cudaErrorInvalidValue;
   }
-  if (rows < 1 || !a.queue) return cudaErrorInvalidValue;
-  const int valid = kSweepCols - 4 * k;
-  const long long strips = (a.W + valid - 1) / valid, bands = (a.H + rows - 1) / rows;
-  const long long units = strips * bands;
-  if (units > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  if (rows < 1 || tail_rows < 0 || !a.queue) return cudaErrorInvalidValue;
   const size_t smem = sweep_smem_bytes(flux_storage, ring);
   // one wave of persistent CTAs (occupancy of this instantiation, queried once)
   static std::mutex mu;
@@ -510,6 +532,23 @@ cudaError_t launch_sweep_step(int k, int rows, int ring, int flux_storage, const
   cudaGetDevice(&dev);
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
     sms = 1;
+  const int valid = kSweepCols - 4 * k;
+  const long long strips = (a.W + valid - 1) / valid;
+  // Band partition: with a tail, about one short unit per resident warp ends
+  // the queue (at most half of the rows).
+  SweepBands sb{};
+  sb.tall = rows;
+  sb.tail = tail_rows > 0 ? tail_rows : rows;
+  long long tail_bands = 0;
+  if (tail_rows > 0) {
+    const long long warps = (long long)per_sm * sms * kSweepWarps;
+    tail_bands = std::min<long long>((warps + strips - 1) / strips, a.H / (2LL * tail_rows));
+  }
+  sb.tall_end = a.H - (int)(tail_bands * sb.tail);
+  sb.tall_count = (sb.tall_end + rows - 1) / rows;
+  sb.count = sb.tall_count + (int)tail_bands;
+  const long long units = strips * sb.count;
+  if (units > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
   const long long blocks =
       std::min<long long>((units + kSweepWarps - 1) / kSweepWarps, (long long)per_sm * sms);
   cudaLaunchAttribute attr[1];
@@ -522,9 +561,9 @@ cudaError_t launch_sweep_step(int k, int rows, int ring, int flux_storage, const
   cfg.stream = s;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  using Fn = void (*)(const float*, const float*, const void*, StepArgs, int);
+  using Fn = void (*)(const float*, const float*, const void*, StepArgs, SweepBands);
   const cudaError_t e =
-      cudaLaunchKernelEx(&cfg, reinterpret_cast<Fn>(const_cast<void*>(fn)), b, d, f, a, rows);
+      cudaLaunchKernelEx(&cfg, reinterpret_cast<Fn>(const_cast<void*>(fn)), b, d, f, a, sb);
   count_launch();
   return e;
 }

@@ -137,6 +137,13 @@ def test_variant_table(tws):
             assert kind == tws.VARIANT_SWEEP and 2 <= k <= 4 and tx == 64 - 4 * k and smem > 0
     assert any(x[5] == tws.VARIANT_SWEEP for x in v)
     assert tws.lib().tws_variant_kind(len(v)) == tws.ERR_INVALID
+    # sweeps with a tail of short bands end their queue on units shorter
+    # than the tall bands; every other variant has none
+    tails = [tws.variant_tail_rows(i) for i in range(len(v))]
+    assert any(t > 0 for t in tails)
+    for (k, tx, ty, stages, smem, kind), t in zip(v, tails):
+        assert t == 0 or (kind == tws.VARIANT_SWEEP and 0 < t < ty)
+    assert tws.lib().tws_variant_tail_rows(len(v)) == tws.ERR_INVALID
     # entries 0..3 are the defaults for K = 1..4
     assert [v[i][0] for i in range(4)] == [1, 2, 3, 4]
     assert tws.lib().tws_variant_info(len(v), None, None, None, None, None) == tws.ERR_INVALID

@@ -193,7 +193,57 @@ __global__ void flux_from_f32_kernel(const float4* in, int f16, float scale, int
   }
 }
 
+// Rows of packed host-layout arrays to or from rows of the pitched state, up
+// to four arrays in one launch (a null source clears its destination).  Each
+// thread moves 16 bytes where both rows allow it, else 4.
+__global__ void __launch_bounds__(256) stage_rows_kernel(StageRows sr, int H) {
+  const unsigned stride = gridDim.x * blockDim.x;
+  for (int a = 0; a < sr.n; ++a) {
+    const int vec = sr.vec[a];  // floats per item: 4 or 1
+    const unsigned per_row = (unsigned)(sr.row_floats[a] / vec);
+    const unsigned items = per_row * (unsigned)H;
+    const float* __restrict__ src = sr.src[a];
+    float* __restrict__ dst = sr.dst[a];
+    const size_t sp = (size_t)sr.src_pitch[a], dp = (size_t)sr.dst_pitch[a];
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < items; i += stride) {
+      const unsigned y = i / per_row, x = (i - y * per_row) * vec;
+      float* o = dst + y * dp + x;
+      if (vec == 4) {
+        const float4 v = src ? __ldcs(reinterpret_cast<const float4*>(src + y * sp + x))
+                             : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        __stcs(reinterpret_cast<float4*>(o), v);
+      } else {
+        *o = src ? src[y * sp + x] : 0.0f;
+      }
+    }
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_stage_rows(const StageRows& sr_in, int H, cudaStream_t st) {
+  StageRows sr = sr_in;
+  long long most = 0;
+  for (int a = 0; a < sr.n; ++a) {
+    const bool aligned = sr.row_floats[a] % 4 == 0 && sr.src_pitch[a] % 4 == 0 &&
+                         sr.dst_pitch[a] % 4 == 0 &&
+                         reinterpret_cast<uintptr_t>(sr.src[a]) % 16 == 0 &&
+                         reinterpret_cast<uintptr_t>(sr.dst[a]) % 16 == 0;
+    sr.vec[a] = aligned ? 4 : 1;
+    const long long items = (long long)(sr.row_floats[a] / sr.vec[a]) * H;
+    if (items > 0x7fffffffLL) return cudaErrorInvalidValue;  // 32-bit item index
+    most = std::max(most, items);
+  }
+  if (most == 0) return cudaSuccess;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
+    sms = 1;
+  const long long blocks = std::min<long long>((most + 255) / 256, 8LL * sms);
+  stage_rows_kernel<<<(unsigned)blocks, 256, 0, st>>>(sr, H);
+  count_launch();
+  return cudaGetLastError();
+}
 
 DevSource make_dev_source(const tws_source& s) {
   DevSource r{};

@@ -856,7 +856,6 @@ TWS_API int tws_upload_async(tws_grid* g, const float* b, const float* d, const 
   if (const int rc = ensure_io(g)) return rc;
   const IoStaging s = io_staging(g);
   const size_t m = (size_t)g->W * g->H, n = (size_t)g->pitch * g->H;
-  const size_t row = (size_t)g->W * 4, pitch = (size_t)g->pitch * 4;
   // host -> staging on the upload stream, once the previous upload has left
   // the staging
   TWS_CUDA(g, cudaStreamWaitEvent(g->io_up, g->up_consumed, 0), "upload order");
@@ -866,30 +865,30 @@ TWS_API int tws_upload_async(tws_grid* g, const float* b, const float* d, const 
   if (f)
     TWS_CUDA(g, cudaMemcpyAsync(s.up_f, f, m * 16, cudaMemcpyHostToDevice, g->io_up), "upload flux");
   TWS_CUDA(g, cudaEventRecord(g->up_copied, g->io_up), "upload order");
-  // staging -> state in the grid's stream order
+  // staging -> state in the grid's stream order: one copy launch on the SMs
+  // (terrain, depth, FP32 flux, the cleared flow map)
   TWS_CUDA(g, cudaStreamWaitEvent(g->stream, g->up_copied, 0), "upload order");
   g->cur = 0;
-  TWS_CUDA(g, cudaMemcpy2DAsync(g->b, pitch, s.up_b, row, row, g->H, cudaMemcpyDeviceToDevice,
-                                g->stream),
-           "stage terrain");
+  const int P = g->pitch, W = g->W;
+  StageRows sr{};
+  sr.add(s.up_b, W, g->b, P, W);
   if (d)
-    TWS_CUDA(g, cudaMemcpy2DAsync(g->d[0], pitch, s.up_d, row, row, g->H, cudaMemcpyDeviceToDevice,
-                                  g->stream),
-             "stage depth");
+    sr.add(s.up_d, W, g->d[0], P, W);
   else
-    TWS_CUDA(g, cudaMemsetAsync(g->d[0], 0, n * 4, g->stream), "clear depth");
-  if (f && g->flux_storage == TWS_FLUX_F32)
-    TWS_CUDA(g, cudaMemcpy2DAsync(g->f[0], (size_t)g->pitch * 16, s.up_f, (size_t)g->W * 16,
-                                  (size_t)g->W * 16, g->H, cudaMemcpyDeviceToDevice, g->stream),
-             "stage flux");
-  else if (f)
+    sr.add(nullptr, P, g->d[0], P, P);
+  const bool f32 = g->flux_storage == TWS_FLUX_F32;
+  if (f32)
+    sr.add(f ? s.up_f : nullptr, f ? 4 * W : 4 * P, reinterpret_cast<float*>(g->f[0]), 4 * P,
+           f ? 4 * W : 4 * P);
+  sr.add(nullptr, 2 * P, reinterpret_cast<float*>(g->v), 2 * P, 2 * P);
+  TWS_CUDA(g, launch_stage_rows(sr, g->H, g->stream), "stage state");
+  if (!f32 && f)
     TWS_CUDA(g, launch_flux_from_f32(s.up_f, g->flux_storage, g->flux_scale, g->W, g->H, g->pitch,
                                      g->f[0], g->stream),
              "stage flux");
-  else
+  else if (!f32)
     TWS_CUDA(g, cudaMemsetAsync(g->f[0], 0, n * flux_bytes_per_cell(g->flux_storage), g->stream),
              "clear flux");
-  TWS_CUDA(g, cudaMemsetAsync(g->v, 0, n * 8, g->stream), "clear velocity");
   TWS_CUDA(g, cudaEventRecord(g->up_consumed, g->stream), "upload order");
   return TWS_OK;
 }
@@ -899,26 +898,21 @@ TWS_API int tws_download_async(tws_grid* g, float* d, float* f, float* v) {
   if (const int rc = ensure_io(g)) return rc;
   const IoStaging s = io_staging(g);
   const size_t m = (size_t)g->W * g->H;
-  const size_t row = (size_t)g->W * 4, pitch = (size_t)g->pitch * 4;
   // state -> staging in the grid's stream order, once the previous download
   // has left the staging
   TWS_CUDA(g, cudaStreamWaitEvent(g->stream, g->down_copied, 0), "download order");
-  if (d)
-    TWS_CUDA(g, cudaMemcpy2DAsync(s.down_d, row, g->d[g->cur], pitch, row, g->H,
-                                  cudaMemcpyDeviceToDevice, g->stream),
-             "stage depth");
-  if (f && g->flux_storage == TWS_FLUX_F32)
-    TWS_CUDA(g, cudaMemcpy2DAsync(s.down_f, (size_t)g->W * 16, g->f[g->cur], (size_t)g->pitch * 16,
-                                  (size_t)g->W * 16, g->H, cudaMemcpyDeviceToDevice, g->stream),
-             "stage flux");
-  else if (f)
+  const int P = g->pitch, W = g->W;
+  const bool f32 = g->flux_storage == TWS_FLUX_F32;
+  StageRows sr{};
+  if (d) sr.add(g->d[g->cur], P, s.down_d, W, W);
+  if (f && f32)
+    sr.add(reinterpret_cast<const float*>(g->f[g->cur]), 4 * P, s.down_f, 4 * W, 4 * W);
+  if (v) sr.add(reinterpret_cast<const float*>(g->v), 2 * P, s.down_v, 2 * W, 2 * W);
+  TWS_CUDA(g, launch_stage_rows(sr, g->H, g->stream), "stage state");
+  if (f && !f32)
     TWS_CUDA(g, launch_flux_to_f32(g->f[g->cur], g->flux_storage, 1.0f / g->flux_scale, g->W, g->H,
                                    g->pitch, s.down_f, g->stream),
              "stage flux");
-  if (v)
-    TWS_CUDA(g, cudaMemcpy2DAsync(s.down_v, (size_t)g->W * 8, g->v, (size_t)g->pitch * 8,
-                                  (size_t)g->W * 8, g->H, cudaMemcpyDeviceToDevice, g->stream),
-             "stage velocity");
   TWS_CUDA(g, cudaEventRecord(g->down_staged, g->stream), "download order");
   // staging -> host on the download stream
   TWS_CUDA(g, cudaStreamWaitEvent(g->io_down, g->down_staged, 0), "download order");

@@ -161,6 +161,26 @@ cudaError_t launch_flux_to_f32(const void* f, int flux_storage, float inv_scale,
                                int pitch, float* out_packed, cudaStream_t st);
 cudaError_t launch_flux_from_f32(const float* in_packed, int flux_storage, float scale, int W,
                                  int H, int pitch, void* f, cudaStream_t st);
+// Up to four row copies between packed arrays and the pitched state in one
+// launch on the SMs (device-to-device copies on the copy engines are several
+// times slower); a null source writes zeros.  Pitches and row lengths in
+// floats; `vec` is filled by the launcher.
+struct StageRows {
+  const float* src[4];
+  float* dst[4];
+  int row_floats[4], src_pitch[4], dst_pitch[4], vec[4];
+  int n;
+  void add(const float* s, int sp, float* d, int dp, int floats) {
+    src[n] = s;
+    dst[n] = d;
+    src_pitch[n] = sp;
+    dst_pitch[n] = dp;
+    row_floats[n] = floats;
+    vec[n] = 1;
+    ++n;
+  }
+};
+cudaError_t launch_stage_rows(const StageRows& sr, int H, cudaStream_t st);
 
 // tws_export.cu
 cudaError_t launch_surface(const float* b, const float* d, const float2* v, int W, int H,

@@ -208,6 +208,11 @@ TWS_API int tws_variant_tail_rows(int variant);
 /* Pin a variant for this grid (-1: automatic -- the tuned choice for this
  * grid shape if tws_autotune ran for one, else the steps-per-launch setting). */
 TWS_API int tws_set_variant(tws_grid* grid, int variant);
+/* The variant that tws_step launches for this grid now: the pinned one, the
+ * tuned one, or the automatic choice for its size and flux storage (a call's
+ * remainder of fewer steps than the variant's depth runs a shallower tile
+ * variant).  The resident kernel (tws_set_resident) is not a variant. */
+TWS_API int tws_current_variant(tws_grid* grid, int* variant);
 
 /* Failure detection (no reference counterpart: the reference's shaders have
  * no waits that can run out).  A step kernel waits on a barrier for each of

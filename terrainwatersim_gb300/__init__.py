@@ -111,6 +111,7 @@ def _declare(L):
         "tws_variant_info": ([i, vp, vp, vp, vp, vp], i),
         "tws_variant_kind": ([i], i),
         "tws_variant_tail_rows": ([i], i),
+        "tws_current_variant": ([vp, vp], i),
         "tws_set_variant": ([vp, i], i),
         "tws_set_wait_limit": ([vp, C.c_longlong], i),
         "tws_test_drop_tile_loads": ([vp, i], i),
@@ -378,6 +379,12 @@ class Grid:
 
     def set_variant(self, variant: int):
         _check(lib().tws_set_variant(self._h, variant), self._h)
+
+    def current_variant(self) -> int:
+        """The variant tws_step launches for this grid now (tws_current_variant)."""
+        v = C.c_int()
+        _check(lib().tws_current_variant(self._h, C.byref(v)), self._h)
+        return v.value
 
     def set_wait_limit(self, sm_cycles: int):
         """SM clocks a tile-load wait may take before the kernel gives up

@@ -599,6 +599,12 @@ TWS_API int tws_variant_info(int i, int* k, int* tx, int* ty, int* stages, size_
   return TWS_OK;
 }
 
+TWS_API int tws_current_variant(tws_grid* g, int* variant) {
+  if (!g || !variant) return TWS_ERR_INVALID;
+  *variant = chosen_variant(g);
+  return TWS_OK;
+}
+
 TWS_API int tws_variant_tail_rows(int i) {
   if (i < 0 || i >= step_variant_count()) return TWS_ERR_INVALID;
   return step_variant(i).kind == kKindSweep ? step_variant(i).ry_tail : 0;

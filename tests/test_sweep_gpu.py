@@ -146,3 +146,46 @@ def test_large_fp32_grid_default_is_bitexact(tws, oracle):
     assert_bitexact(gd, od, "depth")
     assert_bitexact(gf, of, "flux")
     assert_bitexact(gv, ov, "flow map")
+
+
+def test_tail_bands_bitexact(tws, oracle):
+    """Sweep variants whose queue ends in short bands, on a grid with several
+    full tall bands, a partial one and the tail: sources straddle the band
+    edges; every result is the oracle's."""
+    W, H = 1000, 2100
+    b, d, f = rough_state(W, H, 77)
+    p = tws.params_physical(boundary=tws.BOUNDARY_CLOSED)
+    srcs = [(tws.SOURCE_DISK, 500, 384, 30, 0.05), (tws.SOURCE_DISK, 130, 1090, 40, 0.03),
+            (tws.SOURCE_BRUSH, 800.0, 1700.0, 900.0, 0.5)]
+    steps = 7
+    od, of, ov = oracle_run(oracle, b, d, f, p.as_tuple(), srcs, steps, oracle.BOUNDARY_CLOSED)
+    tails = [vi for vi in sweep_variants(tws) if tws.variant_tail_rows(vi) > 0]
+    assert tails
+    for vi in tails:
+        gd, gf, gv, _ = gpu_run(tws, vi, b, d, f, p, srcs, steps)
+        assert_bitexact(gd, od, f"depth variant {vi}")
+        assert_bitexact(gf, of, f"flux variant {vi}")
+        assert_bitexact(gv, ov, f"flow map variant {vi}")
+
+
+@pytest.mark.parametrize("N,flux,k,rows,tail", [
+    (4096, 0, 3, 40, 0),      # FP32: three-step sweep, uniform 40-row bands
+    (8192, 0, 3, 192, 48),    # larger grids: tall bands ending in short ones
+    (4096, 1, 2, None, None), # FP16 below 48 Mi cells: the tiles
+    (8192, 1, 2, 96, 32),     # FP16 from 48 Mi cells: the two-step sweep
+])
+def test_default_variant_ladder(tws, N, flux, k, rows, tail):
+    """The automatic choice per size and flux storage (the band heights are
+    the measured rungs for a 152-SM GB300)."""
+    import torch
+    p = tws.params_physical(boundary=tws.BOUNDARY_CLOSED)
+    with tws.Grid(N, N, p, flux) as g:
+        vi = g.current_variant()
+    v = tws.variants()[vi]
+    assert v[0] == k
+    if rows is None:
+        assert v[5] == tws.VARIANT_TILE
+        return
+    assert v[5] == tws.VARIANT_SWEEP
+    if torch.cuda.get_device_properties(0).multi_processor_count == 152:
+        assert (v[2], tws.variant_tail_rows(vi)) == (rows, tail)

@@ -114,7 +114,7 @@ int step_variant_for(int k, int flux_storage);
 // The automatic choice for grids of at least kLargeGridCells cells (FP16
 // flux: kLargeF16Cells), or -1.
 constexpr long long kLargeGridCells = 12LL << 20;
-constexpr long long kLargeF16Cells = 48LL << 20;
+constexpr long long kLargeF16Cells = 32LL << 20;
 int step_variant_large_grid(int flux_storage, int W, int H);
 // Tile variants read through the tensor maps, stream variants through the
 // raw pointers (b, d, f of the current state).
@@ -128,7 +128,7 @@ cudaError_t launch_sweep_step(int k, int rows, int tail_rows, int ring, int flux
                               const float* b,
                               const float* d, const void* f, const StepArgs& a, cudaStream_t s);
 constexpr int kSweepCtaThreads = 128;  // four warps, each its own sweep
-size_t sweep_smem_bytes(int flux_storage, int ring);
+size_t sweep_smem_bytes(int k, int flux_storage, int ring);
 int sweep_valid_columns(int k);
 // tws_stream.cu
 cudaError_t launch_stream_step(int ry, int flux_storage, const float* b, const float* d,

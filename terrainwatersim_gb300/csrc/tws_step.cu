@@ -902,27 +902,23 @@ struct VariantTable {
     // FP32 (Gcell-steps/s): K = 3 with 40-row bands 199.7, 48 195.0, 32 194.1,
     // 64 186.8, 96 175.6, 128 168.4; K = 2 172 with 24-48-row bands; K = 4
     // 162 with 64-row bands.  A ring of 8 rows is no faster than 4.
-    add_sweep(2, 32, 4);   // 23
-    add_sweep(2, 48, 4);   // 24
-    add_sweep(3, 32, 4);   // 25
-    add_sweep(3, 40, 4);   // 26  the default for large FP32 grids
-    add_sweep(3, 48, 4);   // 27
-    add_sweep(3, 64, 4);   // 28
-    add_sweep(4, 64, 4);   // 29
+    add_sweep(2, 32, 3);   // 23
+    add_sweep(2, 48, 3);   // 24
+    add_sweep(3, 32, 3);   // 25
+    add_sweep(3, 40, 3);   // 26  the default for large FP32 grids
+    add_sweep(3, 48, 3);   // 27
+    add_sweep(3, 64, 3);   // 28
+    add_sweep(4, 64, 3);   // 29
     // Taller bands, the last ones short (the tail: about one short unit per
     // resident warp ends the work queue).  Tall bands recompute fewer halo
     // rows per output row, and the tail keeps the launch's end short.
-    // FP32, K = 3 (Gcell-steps/s): 6144^2 80/32 223.6 (40: 205.8); 8192^2
-    // 192/48 248.7; 12288^2 384/64 253.4; 16384^2 256/64 256.2, 384/64 253.6
-    // (64: 233.9).  FP16, K = 2: 8192^2 96/32 232.1; 12288^2 192/48 245.2;
-    // 16384^2 192/48 249.9 (48: 226.2).
-    add_sweep(3, 80, 4, 32);   // 30
-    add_sweep(3, 128, 4, 48);  // 31
-    add_sweep(3, 192, 4, 48);  // 32
-    add_sweep(3, 256, 4, 64);  // 33
-    add_sweep(3, 384, 4, 64);  // 34
-    add_sweep(2, 96, 4, 32);   // 35
-    add_sweep(2, 192, 4, 48);  // 36
+    // K = 3 (Gcell-steps/s, FP32 / FP16 flux): 8192^2 192/48 253.1 / 237.6,
+    // 256/64 255.8 / 231.1; 16384^2 256/64 266.2 / 254.3 (64 rows: 233.9 /
+    // 228.3).
+    add_sweep(3, 80, 3, 32);   // 30
+    add_sweep(3, 128, 3, 48);  // 31
+    add_sweep(3, 192, 3, 48);  // 32
+    add_sweep(3, 256, 3, 64);  // 33
   }
   void add_sweep(int k, int rows, int ring, int tail_rows = 0) {
     VariantEntry s{};
@@ -934,7 +930,7 @@ struct VariantTable {
     s.v.kind = kKindSweep;
     s.v.ry = rows;
     s.v.ring = ring;
-    s.v.smem = sweep_smem_bytes(TWS_FLUX_F32, ring);
+    s.v.smem = sweep_smem_bytes(k, TWS_FLUX_F32, ring);
     e[n] = s;
     if (n < kMax) ++n;
   }
@@ -985,23 +981,17 @@ int step_variant_count() { return table().n; }
 const StepVariant& step_variant(int i) { return table().e[i].v; }
 
 int step_variant_large_grid(int flux_storage, int W, int H) {
-  // FP32 flux: the three-step row sweep (4096^2: 40-row bands, 196.8-199.7
-  // Gcell-steps/s against 192-193 for the two-step tiles).  FP16 flux: the
-  // two-step sweep from kLargeF16Cells on; below it the tiles are faster
-  // (4096^2: 203.1 against 191.0).  The band height is the tallest on a
-  // ladder that leaves enough units per resident warp for the work queue to
-  // balance: 3.5 for K = 3 (three CTAs of four warps per SM), 5 for K = 2
-  // (four CTAs per SM); the thresholds are measured on 4096^2 to 16384^2.
+  // The three-step row sweep: FP32 flux from kLargeGridCells on (4096^2:
+  // 40-row bands, 202.8 Gcell-steps/s against 193.4 for the two-step tiles),
+  // FP16 flux from kLargeF16Cells on (6144^2: 219.4 against 209.0 for the
+  // FP16 tiles; below it the tiles are as fast or faster: 4096^2 203.7
+  // against 184.9).  The band height is the tallest rung of a
+  // ladder that leaves at least 2.5 units per resident warp (four CTAs of four
+  // warps per SM), measured on 4096^2 to 16384^2.
   const long long cells = (long long)W * H;
   if (cells < kLargeGridCells) return -1;
-  const bool f32 = flux_storage == TWS_FLUX_F32;
-  if (!f32 && cells < kLargeF16Cells) return -1;
-  const int k = f32 ? 3 : 2;
-  static const int kLadder3[][2] = {{40, 0}, {80, 32}, {128, 48}, {192, 48}, {256, 64}, {384, 64}};
-  static const int kLadder2[][2] = {{48, 0}, {96, 32}, {192, 48}};
-  const int(*ladder)[2] = f32 ? kLadder3 : kLadder2;
-  const int rungs = f32 ? 6 : 3;
-  const double per_warp = f32 ? 3.5 : 5.0;
+  if (flux_storage != TWS_FLUX_F32 && cells < kLargeF16Cells) return -1;
+  static const int kLadder[][2] = {{40, 0}, {80, 32}, {128, 48}, {192, 48}, {256, 64}};
   static int sms = 0;
   if (sms == 0) {
     int dev = 0, n = 0;
@@ -1010,15 +1000,16 @@ int step_variant_large_grid(int flux_storage, int W, int H) {
               ? n
               : 1;
   }
-  const double warps = (double)sms * (f32 ? 3 : 4) * (kSweepCtaThreads / 32);
-  const long long strips = (W + sweep_valid_columns(k) - 1) / sweep_valid_columns(k);
+  const double warps = (double)sms * 4 * (kSweepCtaThreads / 32);
+  const long long strips = (W + sweep_valid_columns(3) - 1) / sweep_valid_columns(3);
   int pick = -1;
-  for (int r = 0; r < rungs; ++r) {
-    const long long units = strips * ((H + ladder[r][0] - 1) / ladder[r][0]);
-    if (r > 0 && units < per_warp * warps) break;
+  for (int r = 0; r < (int)(sizeof(kLadder) / sizeof(kLadder[0])); ++r) {
+    const long long units = strips * ((H + kLadder[r][0] - 1) / kLadder[r][0]);
+    if (r > 0 && units < 2.5 * warps) break;
     for (int i = 0; i < step_variant_count(); ++i) {
       const StepVariant& e = step_variant(i);
-      if (e.kind == kKindSweep && e.k == k && e.ry == ladder[r][0] && e.ry_tail == ladder[r][1])
+      if (e.kind == kKindSweep && e.k == 3 && e.ry == kLadder[r][0] &&
+          e.ry_tail == kLadder[r][1])
         pick = i;
     }
   }

@@ -89,7 +89,7 @@ __device__ __forceinline__ float2 sum_products(float2 p, float2 q) {
   return make_float2(fadd(p.x, q.x), fadd(p.y, q.y));
 }
 
-template <bool F16, int P>
+template <int K, bool F16, int P>
 struct SweepRing {
   // one row of a lane's ring: b and d of its two cells, then the flux records
   // (FP32: the first cells of all lanes, then the second cells, so that a
@@ -98,7 +98,12 @@ struct SweepRing {
   static constexpr int D = 256;  // 64 floats
   static constexpr int F = 512;  // FP32: 2 x 32 float4; FP16: 32 x 16 bytes
   static constexpr int ROW = F + (F16 ? 512 : 1024);
-  static constexpr int WARP = ROW * P;  // P rows: P - 1 in flight
+  static constexpr int RING = ROW * P;  // P rows: P - 1 in flight
+  // The new outflows of each level's last three rows (the row computed in
+  // this iteration and the two before it), one 1 KB slot per row: each
+  // lane's (+x, -x) pairs at 16 * lane, its (+y, -y) pairs at 512 + 16 * lane.
+  static constexpr int NSLOT = 1024;
+  static constexpr int WARP = RING + K * 3 * NSLOT;
 };
 
 template <int K, bool F16, bool INTERIOR, int P>
@@ -108,7 +113,7 @@ __device__ __forceinline__ void sweep_unit(const StepArgs& a, const float* __res
                                            float* __restrict__ d_out, void* __restrict__ f_out,
                                            float2* __restrict__ v_out, unsigned char* ring,
                                            int xs, int y0, int R, uint32_t mask) {
-  using RG = SweepRing<F16, P>;
+  using RG = SweepRing<K, F16, P>;
   constexpr int HALO = 2 * K;
   const int lane = threadIdx.x & 31;
   const int W = a.W, H = a.H;
@@ -198,13 +203,33 @@ __device__ __forceinline__ void sweep_unit(const StepArgs& a, const float* __res
   float2 H0[K], H1[K];  // h of rows ys - 1 and ys of level s's outflow row ys
   float2 D0[K], D1[K];  // d of rows ys - 1 and ys
   float2 B0[K], B1[K];  // terrain of rows ys - 1 and ys (it travels with the rows)
-  Flux2 N1[K], N2[K];   // new outflow of rows ys - 1 and ys - 2
+  // The new outflows of rows ys - 1 and ys - 2 live in shared memory (three
+  // slots per level, rotating with the iteration), which leaves registers for
+  // four CTAs per SM.  A lane reads back only what it wrote.
+  unsigned char* const nring = ring + RG::RING;
+  auto n_slot = [&](int s, int q) { return nring + (s * 3 + q) * RG::NSLOT; };
+  auto store_n = [&](int s, int q, const Flux2& v) {
+    unsigned char* sl = n_slot(s, q);
+    *reinterpret_cast<float4*>(sl + 16 * lane) = make_float4(v.x.x, v.x.y, v.y.x, v.y.y);
+    *reinterpret_cast<float4*>(sl + 512 + 16 * lane) = make_float4(v.z.x, v.z.y, v.w.x, v.w.y);
+  };
+  auto load_n = [&](int s, int q) -> Flux2 {
+    const unsigned char* sl = n_slot(s, q);
+    const float4 p = *reinterpret_cast<const float4*>(sl + 16 * lane);
+    const float4 m = *reinterpret_cast<const float4*>(sl + 512 + 16 * lane);
+    return Flux2{make_float2(p.x, p.y), make_float2(p.z, p.w), make_float2(m.x, m.y),
+                 make_float2(m.z, m.w)};
+  };
+  auto load_n_z = [&](int s, int q) -> float2 {  // the +y pair alone
+    return *reinterpret_cast<const float2*>(n_slot(s, q) + 512 + 16 * lane);
+  };
   const float2 z2 = make_float2(0.0f, 0.0f);
 #pragma unroll
   for (int s = 0; s < K; ++s) {
     H0[s] = H1[s] = D0[s] = D1[s] = B0[s] = B1[s] = z2;
-    N1[s] = N2[s] = zero_flux();
+    for (int q = 0; q < 3; ++q) store_n(s, q, zero_flux());
   }
+  int q_cur = 0, q_prev = 2, q_prev2 = 1;  // slots of rows ys, ys - 1, ys - 2
 
   // the ring: rows 0 .. P - 2 in flight before the loop
 #pragma unroll
@@ -290,17 +315,26 @@ __device__ __forceinline__ void sweep_unit(const StepArgs& a, const float* __res
         if (!in1) nf.x.y = nf.y.y = nf.z.y = nf.w.y = 0.0f;
       }
 
+      store_n(s, q_cur, nf);
+
       // -- depth and flow map of row ys - 1, flowApply.comp:32-52
       const int yd = ys - 1;
-      const Flux2 own = N1[s];
+      const Flux2 own = load_n(s, q_prev);
       const float2 X1 = make_float2(own.y.y, __shfl_down_sync(0xffffffffu, own.y.x, 1));
       const float2 X0 = make_float2(__shfl_up_sync(0xffffffffu, own.x.y, 1), own.x.x);
-      const float2 Y1 = nf.w, Y0 = N2[s].z;
+      Flux2 handoff;  // new outflow of row ys - 2: level s + 1's input
+      float2 Y0;
+      if (s + 1 < K) {
+        handoff = load_n(s, q_prev2);
+        Y0 = handoff.z;
+      } else {
+        Y0 = load_n_z(s, q_prev2);
+      }
+      const float2 Y1 = nf.w;
       const float2 in = fadd2(fadd2(fadd2(X1, X0), Y1), Y0);
       const float2 out = fadd2(fadd2(fadd2(own.x, own.y), own.z), own.w);
       const float2 dn = max0x2(sum_products(D0[s], fmul2(fsub2(in, out), cc2)));
-      const Flux2 handoff = N2[s];  // new outflow of row ys - 2: level s + 1's input
-      const float2 b_d = B0[s];     // terrain of the depth row
+      const float2 b_d = B0[s];  // terrain of the depth row
       // shift the windows
       H0[s] = hc;
       H1[s] = hp;
@@ -308,8 +342,6 @@ __device__ __forceinline__ void sweep_unit(const StepArgs& a, const float* __res
       D1[s] = d_in;
       B0[s] = B1[s];
       B1[s] = b_in;
-      N2[s] = own;
-      N1[s] = nf;
       if (s + 1 < K) {
         // level s + 1's input row yd: next step's sources, h = d + b
         const bool yd_in = INTERIOR || (yd >= 0 && yd < H);
@@ -365,6 +397,11 @@ __device__ __forceinline__ void sweep_unit(const StepArgs& a, const float* __res
         }
       }
     }
+    // the row of this iteration becomes ys - 1, its predecessor ys - 2
+    const int q_free = q_prev2;
+    q_prev2 = q_prev;
+    q_prev = q_cur;
+    q_cur = q_free;
   }
   copy_wait<0>();
 }
@@ -416,11 +453,11 @@ __device__ __forceinline__ void sweep_band(const SweepBands& sb, int H, int i, i
 // Persistent warps (one wave): each takes units (strip, band) from the grid's
 // queue until none is left, so warps that drew cheap units take more of them.
 template <int K, bool F16, int P, bool TAIL>
-__global__ void __launch_bounds__(kSweepThreads, (K <= 2 ? 4 : (K == 3 ? 3 : 2)))
+__global__ void __launch_bounds__(kSweepThreads, (K <= 3 ? 4 : 2))
     sweep_kernel(const float* __restrict__ b, const float* __restrict__ d,
                  const void* __restrict__ f, const __grid_constant__ StepArgs a,
                  const SweepBands sb) {
-  using RG = SweepRing<F16, P>;
+  using RG = SweepRing<K, F16, P>;
   constexpr int VALID = kSweepCols - 4 * K;
   extern __shared__ __align__(128) unsigned char sweep_smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -491,24 +528,25 @@ const void* sweep_fn(int flux_storage, bool tail) {
 
 int sweep_valid_columns(int k) { return kSweepCols - 4 * k; }
 
-size_t sweep_smem_bytes(int flux_storage, int ring) {
-  return (size_t)kSweepWarps * ring * (flux_storage == TWS_FLUX_F16 ? SweepRing<true, 1>::ROW
-                                                                    : SweepRing<false, 1>::ROW);
+size_t sweep_smem_bytes(int k, int flux_storage, int ring) {
+  const size_t row = flux_storage == TWS_FLUX_F16 ? SweepRing<1, true, 1>::ROW
+                                                  : SweepRing<1, false, 1>::ROW;
+  return (size_t)kSweepWarps * (ring * row + (size_t)k * 3 * SweepRing<1, false, 1>::NSLOT);
 }
 
 cudaError_t launch_sweep_step(int k, int rows, int tail_rows, int ring, int flux_storage,
                               const float* b, const float* d, const void* f, const StepArgs& a,
                               cudaStream_t s) {
   const void* fn = nullptr;
-  if (ring != 4) return cudaErrorInvalidValue;
+  if (ring != 3) return cudaErrorInvalidValue;
   switch (k) {
-    case 2: fn = sweep_fn<2, 4>(flux_storage, tail_rows > 0); break;
-    case 3: fn = sweep_fn<3, 4>(flux_storage, tail_rows > 0); break;
-    case 4: fn = sweep_fn<4, 4>(flux_storage, tail_rows > 0); break;
+    case 2: fn = sweep_fn<2, 3>(flux_storage, tail_rows > 0); break;
+    case 3: fn = sweep_fn<3, 3>(flux_storage, tail_rows > 0); break;
+    case 4: fn = sweep_fn<4, 3>(flux_storage, tail_rows > 0); break;
     default: return cudaErrorInvalidValue;
   }
   if (rows < 1 || tail_rows < 0 || !a.queue) return cudaErrorInvalidValue;
-  const size_t smem = sweep_smem_bytes(flux_storage, ring);
+  const size_t smem = sweep_smem_bytes(k, flux_storage, ring);
   // one wave of persistent CTAs (occupancy of this instantiation, queried once)
   static std::mutex mu;
   static std::map<const void*, int> resident;

@@ -171,8 +171,8 @@ def test_tail_bands_bitexact(tws, oracle):
 @pytest.mark.parametrize("N,flux,k,rows,tail", [
     (4096, 0, 3, 40, 0),      # FP32: three-step sweep, uniform 40-row bands
     (8192, 0, 3, 192, 48),    # larger grids: tall bands ending in short ones
-    (4096, 1, 2, None, None), # FP16 below 48 Mi cells: the tiles
-    (8192, 1, 2, 96, 32),     # FP16 from 48 Mi cells: the two-step sweep
+    (4096, 1, 2, None, None), # FP16 below 32 Mi cells: the two-step tiles
+    (8192, 1, 3, 192, 48),    # FP16 from 32 Mi cells: the sweep as for FP32
 ])
 def test_default_variant_ladder(tws, N, flux, k, rows, tail):
     """The automatic choice per size and flux storage (the band heights are

@@ -262,6 +262,19 @@ __device__ __forceinline__ void sweep_unit(const StepArgs& a, const float* __res
     for (int s = 0; s < K; ++s) {
       const int ys = r - 2 * s - 1;  // this level's outflow row
       const bool ys_in = INTERIOR || (ys >= 0 && ys < H);
+      // this level's outflow rows ys - 1 and ys - 2 from shared memory, read
+      // ahead of the arithmetic that hides their latency (the slots differ
+      // from the one this iteration writes)
+      const Flux2 own = load_n(s, q_prev);
+      Flux2 handoff;  // new outflow of row ys - 2: level s + 1's input
+      float2 Y0;
+      if (s + 1 < K) {
+        handoff = load_n(s, q_prev2);
+        Y0 = handoff.z;
+      } else {
+        Y0 = load_n_z(s, q_prev2);
+      }
+
       // -- outflow of row ys, flowUpdate.comp:34-62
       const float2 hm = H0[s], hc = H1[s], hp = h_in;
       const float2 h_right = make_float2(hc.y, __shfl_down_sync(0xffffffffu, hc.x, 1));
@@ -319,17 +332,8 @@ __device__ __forceinline__ void sweep_unit(const StepArgs& a, const float* __res
 
       // -- depth and flow map of row ys - 1, flowApply.comp:32-52
       const int yd = ys - 1;
-      const Flux2 own = load_n(s, q_prev);
       const float2 X1 = make_float2(own.y.y, __shfl_down_sync(0xffffffffu, own.y.x, 1));
       const float2 X0 = make_float2(__shfl_up_sync(0xffffffffu, own.x.y, 1), own.x.x);
-      Flux2 handoff;  // new outflow of row ys - 2: level s + 1's input
-      float2 Y0;
-      if (s + 1 < K) {
-        handoff = load_n(s, q_prev2);
-        Y0 = handoff.z;
-      } else {
-        Y0 = load_n_z(s, q_prev2);
-      }
       const float2 Y1 = nf.w;
       const float2 in = fadd2(fadd2(fadd2(X1, X0), Y1), Y0);
       const float2 out = fadd2(fadd2(fadd2(own.x, own.y), own.z), own.w);

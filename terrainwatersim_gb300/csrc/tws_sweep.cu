@@ -274,6 +274,13 @@ __device__ __forceinline__ void sweep_unit(const StepArgs& a, const float* __res
       } else {
         Y0 = load_n_z(s, q_prev2);
       }
+      // the parts of the depth update that do not need this row's outflow
+      // (flowApply.comp:32-39): the x inflows and the outflow sum of row
+      // ys - 1, ahead of the outflow's divergent scaling branch
+      const float2 X1 = make_float2(own.y.y, __shfl_down_sync(0xffffffffu, own.y.x, 1));
+      const float2 X0 = make_float2(__shfl_up_sync(0xffffffffu, own.x.y, 1), own.x.x);
+      const float2 in_x = fadd2(X1, X0);
+      const float2 out = fadd2(fadd2(fadd2(own.x, own.y), own.z), own.w);
 
       // -- outflow of row ys, flowUpdate.comp:34-62
       const float2 hm = H0[s], hc = H1[s], hp = h_in;
@@ -332,11 +339,8 @@ __device__ __forceinline__ void sweep_unit(const StepArgs& a, const float* __res
 
       // -- depth and flow map of row ys - 1, flowApply.comp:32-52
       const int yd = ys - 1;
-      const float2 X1 = make_float2(own.y.y, __shfl_down_sync(0xffffffffu, own.y.x, 1));
-      const float2 X0 = make_float2(__shfl_up_sync(0xffffffffu, own.x.y, 1), own.x.x);
       const float2 Y1 = nf.w;
-      const float2 in = fadd2(fadd2(fadd2(X1, X0), Y1), Y0);
-      const float2 out = fadd2(fadd2(fadd2(own.x, own.y), own.z), own.w);
+      const float2 in = fadd2(fadd2(in_x, Y1), Y0);
       const float2 dn = max0x2(sum_products(D0[s], fmul2(fsub2(in, out), cc2)));
       const float2 b_d = B0[s];  // terrain of the depth row
       // shift the windows

@@ -99,11 +99,12 @@ struct SweepRing {
   static constexpr int F = 512;  // FP32: 2 x 32 float4; FP16: 32 x 16 bytes
   static constexpr int ROW = F + (F16 ? 512 : 1024);
   static constexpr int RING = ROW * P;  // P rows: P - 1 in flight
-  // The new outflows of each level's last three rows (the row computed in
-  // this iteration and the two before it), one 1 KB slot per row: each
-  // lane's (+x, -x) pairs at 16 * lane, its (+y, -y) pairs at 512 + 16 * lane.
+  // The new outflows of each level's two previous rows, one 1 KB slot per
+  // row (the row computed in an iteration takes the slot of the older one
+  // once it has been read): each lane's (+x, -x) pairs at 16 * lane, its
+  // (+y, -y) pairs at 512 + 16 * lane.
   static constexpr int NSLOT = 1024;
-  static constexpr int WARP = RING + K * 3 * NSLOT;
+  static constexpr int WARP = RING + K * 2 * NSLOT;
 };
 
 template <int K, bool F16, bool INTERIOR, int P>
@@ -203,11 +204,11 @@ __device__ __forceinline__ void sweep_unit(const StepArgs& a, const float* __res
   float2 H0[K], H1[K];  // h of rows ys - 1 and ys of level s's outflow row ys
   float2 D0[K], D1[K];  // d of rows ys - 1 and ys
   float2 B0[K], B1[K];  // terrain of rows ys - 1 and ys (it travels with the rows)
-  // The new outflows of rows ys - 1 and ys - 2 live in shared memory (three
-  // slots per level, rotating with the iteration), which leaves registers for
+  // The new outflows of rows ys - 1 and ys - 2 live in shared memory (two
+  // slots per level, swapped every iteration), which leaves registers for
   // four CTAs per SM.  A lane reads back only what it wrote.
   unsigned char* const nring = ring + RG::RING;
-  auto n_slot = [&](int s, int q) { return nring + (s * 3 + q) * RG::NSLOT; };
+  auto n_slot = [&](int s, int q) { return nring + (s * 2 + q) * RG::NSLOT; };
   auto store_n = [&](int s, int q, const Flux2& v) {
     unsigned char* sl = n_slot(s, q);
     *reinterpret_cast<float4*>(sl + 16 * lane) = make_float4(v.x.x, v.x.y, v.y.x, v.y.y);
@@ -227,9 +228,9 @@ __device__ __forceinline__ void sweep_unit(const StepArgs& a, const float* __res
 #pragma unroll
   for (int s = 0; s < K; ++s) {
     H0[s] = H1[s] = D0[s] = D1[s] = B0[s] = B1[s] = z2;
-    for (int q = 0; q < 3; ++q) store_n(s, q, zero_flux());
+    for (int q = 0; q < 2; ++q) store_n(s, q, zero_flux());
   }
-  int q_cur = 0, q_prev = 2, q_prev2 = 1;  // slots of rows ys, ys - 1, ys - 2
+  int q_prev = 1, q_prev2 = 0;  // slots of rows ys - 1 and ys - 2
 
   // the ring: rows 0 .. P - 2 in flight before the loop
 #pragma unroll
@@ -263,8 +264,8 @@ __device__ __forceinline__ void sweep_unit(const StepArgs& a, const float* __res
       const int ys = r - 2 * s - 1;  // this level's outflow row
       const bool ys_in = INTERIOR || (ys >= 0 && ys < H);
       // this level's outflow rows ys - 1 and ys - 2 from shared memory, read
-      // ahead of the arithmetic that hides their latency (the slots differ
-      // from the one this iteration writes)
+      // ahead of the arithmetic that hides their latency (row ys - 2's slot
+      // is rewritten only after this read, by the same lane)
       const Flux2 own = load_n(s, q_prev);
       Flux2 handoff;  // new outflow of row ys - 2: level s + 1's input
       float2 Y0;
@@ -335,7 +336,7 @@ __device__ __forceinline__ void sweep_unit(const StepArgs& a, const float* __res
         if (!in1) nf.x.y = nf.y.y = nf.z.y = nf.w.y = 0.0f;
       }
 
-      store_n(s, q_cur, nf);
+      store_n(s, q_prev2, nf);  // row ys takes the slot of ys - 2, read above
 
       // -- depth and flow map of row ys - 1, flowApply.comp:32-52
       const int yd = ys - 1;
@@ -406,10 +407,9 @@ __device__ __forceinline__ void sweep_unit(const StepArgs& a, const float* __res
       }
     }
     // the row of this iteration becomes ys - 1, its predecessor ys - 2
-    const int q_free = q_prev2;
+    const int q_row = q_prev2;
     q_prev2 = q_prev;
-    q_prev = q_cur;
-    q_cur = q_free;
+    q_prev = q_row;
   }
   copy_wait<0>();
 }
@@ -539,7 +539,7 @@ int sweep_valid_columns(int k) { return kSweepCols - 4 * k; }
 size_t sweep_smem_bytes(int k, int flux_storage, int ring) {
   const size_t row = flux_storage == TWS_FLUX_F16 ? SweepRing<1, true, 1>::ROW
                                                   : SweepRing<1, false, 1>::ROW;
-  return (size_t)kSweepWarps * (ring * row + (size_t)k * 3 * SweepRing<1, false, 1>::NSLOT);
+  return (size_t)kSweepWarps * (ring * row + (size_t)k * 2 * SweepRing<1, false, 1>::NSLOT);
 }
 
 cudaError_t launch_sweep_step(int k, int rows, int tail_rows, int ring, int flux_storage,

@@ -6,9 +6,11 @@
 //
 // * A warp owns a strip of 64 columns (two per lane) and sweeps it down a
 //   band of R rows; the warps are persistent and take (strip, band) units
-//   from a per-grid queue, border units first.  Each lane keeps, per time level s = 0..K-1, a rolling
-//   window of the rows that level needs in registers: surface heights h of
-//   three rows, depths and terrain of two rows, new outflows of two rows.
+//   from a per-grid queue, border units first, short bands last.  Each lane
+//   keeps, per time level s = 0..K-1, a rolling window of the rows that level
+//   needs: surface heights h of three rows, depths and terrain of two rows in
+//   registers, the new outflows of two rows in shared memory (the registers
+//   they would take cost a CTA per SM).
 //   Row by row, level s computes the outflow of one row and the depth of the
 //   row above, which is the input row of level s + 1 two rows further up; the
 //   last level writes its depth, flux and flow map.  The y neighbours come

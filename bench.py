@@ -345,7 +345,7 @@ def run_ours(args):
     hb[...] = g.download_terrain()
     g.download(out=(hd, None, None), flux=False, velocity=False)
     g.set_variant(best_v)
-    e2e_steps = max(3, steps // 2)
+    e2e_steps = steps  # the same K bench steps as the headline, each with its copies
     e2e_value = e2e_serial = None
     if not args.no_e2e:
         # pipelined: each bench step queues its upload, its chain and its

@@ -902,23 +902,23 @@ struct VariantTable {
     // FP32 (Gcell-steps/s): K = 3 with 40-row bands 199.7, 48 195.0, 32 194.1,
     // 64 186.8, 96 175.6, 128 168.4; K = 2 172 with 24-48-row bands; K = 4
     // 162 with 64-row bands.  A ring of 8 rows is no faster than 4.
-    add_sweep(2, 32, 3);   // 23
-    add_sweep(2, 48, 3);   // 24
-    add_sweep(3, 32, 3);   // 25
-    add_sweep(3, 40, 3);   // 26  the default for large FP32 grids
-    add_sweep(3, 48, 3);   // 27
-    add_sweep(3, 64, 3);   // 28
-    add_sweep(4, 64, 3);   // 29
+    add_sweep(2, 32, 4);   // 23
+    add_sweep(2, 48, 4);   // 24
+    add_sweep(3, 32, 4);   // 25
+    add_sweep(3, 40, 4);   // 26  the default for large FP32 grids
+    add_sweep(3, 48, 4);   // 27
+    add_sweep(3, 64, 4);   // 28
+    add_sweep(4, 64, 4);   // 29
     // Taller bands, the last ones short (the tail: about one short unit per
     // resident warp ends the work queue).  Tall bands recompute fewer halo
     // rows per output row, and the tail keeps the launch's end short.
     // K = 3 (Gcell-steps/s, FP32 / FP16 flux): 8192^2 192/48 253.1 / 237.6,
     // 256/64 255.8 / 231.1; 16384^2 256/64 266.2 / 254.3 (64 rows: 233.9 /
     // 228.3).
-    add_sweep(3, 80, 3, 32);   // 30
-    add_sweep(3, 128, 3, 48);  // 31
-    add_sweep(3, 192, 3, 48);  // 32
-    add_sweep(3, 256, 3, 64);  // 33
+    add_sweep(3, 80, 4, 32);   // 30
+    add_sweep(3, 128, 4, 48);  // 31
+    add_sweep(3, 192, 4, 48);  // 32
+    add_sweep(3, 256, 4, 64);  // 33
   }
   void add_sweep(int k, int rows, int ring, int tail_rows = 0) {
     VariantEntry s{};

@@ -555,11 +555,11 @@ cudaError_t launch_sweep_step(int k, int rows, int tail_rows, int ring, int flux
                               const float* b, const float* d, const void* f, const StepArgs& a,
                               cudaStream_t s) {
   const void* fn = nullptr;
-  if (ring != 3) return cudaErrorInvalidValue;
+  if (ring != 4) return cudaErrorInvalidValue;
   switch (k) {
-    case 2: fn = sweep_fn<2, 3>(flux_storage, tail_rows > 0); break;
-    case 3: fn = sweep_fn<3, 3>(flux_storage, tail_rows > 0); break;
-    case 4: fn = sweep_fn<4, 3>(flux_storage, tail_rows > 0); break;
+    case 2: fn = sweep_fn<2, 4>(flux_storage, tail_rows > 0); break;
+    case 3: fn = sweep_fn<3, 4>(flux_storage, tail_rows > 0); break;
+    case 4: fn = sweep_fn<4, 4>(flux_storage, tail_rows > 0); break;
     default: return cudaErrorInvalidValue;
   }
   if (rows < 1 || tail_rows < 0 || !a.queue) return cudaErrorInvalidValue;

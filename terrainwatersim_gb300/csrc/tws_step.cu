@@ -992,14 +992,13 @@ int step_variant_large_grid(int flux_storage, int W, int H) {
   if (cells < kLargeGridCells) return -1;
   if (flux_storage != TWS_FLUX_F32 && cells < kLargeF16Cells) return -1;
   static const int kLadder[][2] = {{40, 0}, {80, 32}, {128, 48}, {192, 48}, {256, 64}};
-  static int sms = 0;
-  if (sms == 0) {
+  static const int sms = [] {
     int dev = 0, n = 0;
     cudaGetDevice(&dev);
-    sms = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && n > 0
-              ? n
-              : 1;
-  }
+    return cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && n > 0
+               ? n
+               : 1;
+  }();
   const double warps = (double)sms * 4 * (kSweepCtaThreads / 32);
   const long long strips = (W + sweep_valid_columns(3) - 1) / sweep_valid_columns(3);
   int pick = -1;

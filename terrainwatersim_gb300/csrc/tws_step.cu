@@ -898,10 +898,10 @@ struct VariantTable {
     add<4, 32, 32, 1, true>();  // 20
     add<4, 64, 16, 1, true>();  // 21
     add<3, 64, 32, 1, true>();  // 22
-    // row sweeps: 64-column warp strips, K time levels in registers.  4096^2
-    // FP32 (Gcell-steps/s): K = 3 with 40-row bands 199.7, 48 195.0, 32 194.1,
-    // 64 186.8, 96 175.6, 128 168.4; K = 2 172 with 24-48-row bands; K = 4
-    // 162 with 64-row bands.  A ring of 8 rows is no faster than 4.
+    // row sweeps: 64-column warp strips, K time levels on chip.  4096^2 FP32
+    // (Gcell-steps/s): K = 3 with 32-row bands 211.9, 40 211.6, 48 205.2, 64
+    // 184.4; K = 2 171-173; K = 4 173 with 64-row bands.  A ring of 4 rows is
+    // 0.3-1.5% faster than 3, one of 8 no faster than 4.
     add_sweep(2, 32, 4);   // 23
     add_sweep(2, 48, 4);   // 24
     add_sweep(3, 32, 4);   // 25
@@ -912,9 +912,9 @@ struct VariantTable {
     // Taller bands, the last ones short (the tail: about one short unit per
     // resident warp ends the work queue).  Tall bands recompute fewer halo
     // rows per output row, and the tail keeps the launch's end short.
-    // K = 3 (Gcell-steps/s, FP32 / FP16 flux): 8192^2 192/48 253.1 / 237.6,
-    // 256/64 255.8 / 231.1; 16384^2 256/64 266.2 / 254.3 (64 rows: 233.9 /
-    // 228.3).
+    // K = 3 (Gcell-steps/s, FP32 / FP16 flux): 6144^2 80/32 234.5 / 219.4;
+    // 8192^2 192/48 253.1 / 237.6; 16384^2 128/48 272.0 / 268.8, 192/48
+    // 276.8 / 275.4, 256/64 272.6 / 275.3 (64 rows: 258.8 / 251.4).
     add_sweep(3, 80, 4, 32);   // 30
     add_sweep(3, 128, 4, 48);  // 31
     add_sweep(3, 192, 4, 48);  // 32

@@ -85,6 +85,9 @@ def test_invalid_arguments_rejected_without_touching_the_gpu(tws):
     assert L.tws_io_wait(None) == tws.ERR_INVALID
     assert L.tws_set_resident(None, tws.RESIDENT_AUTO) == tws.ERR_INVALID
     assert L.tws_resident_fits(64, 64, 7) == 0  # no such flux storage
+    v = C.c_int(-7)
+    assert L.tws_current_variant(None, C.byref(v)) == tws.ERR_INVALID and v.value == -7
+    assert L.tws_variant_tail_rows(-1) == tws.ERR_INVALID
 
 
 def test_resident_fits_answers_no_without_a_gpu(tws):

@@ -189,55 +189,6 @@ __global__ void export_kernel4(const float* __restrict__ b, const float* __restr
   }
 }
 
-__device__ __forceinline__ float avg4(float a, float b, float c, float d);
-
-// export_kernel4's work for a 4 x 2 block of cells, plus the two texels of
-// the first mip level those cells make (W % 4 == 0, H even): the level is
-// built from registers instead of re-reading TerrainData.
-__global__ void export_mip1_kernel4(const float* __restrict__ b, const float* __restrict__ d,
-                                    const float2* __restrict__ v, int W, int H, int pitch,
-                                    float4* __restrict__ rgba, __half2* __restrict__ flowmap,
-                                    float4* __restrict__ mip1) {
-  const int x = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
-  const int y = 2 * (blockIdx.y * blockDim.y + threadIdx.y);
-  if (x >= W || y >= H) return;
-  float4 t[2][4];
-#pragma unroll
-  for (int r = 0; r < 2; ++r) {
-    const size_t i = (size_t)(y + r) * pitch + x;
-    const size_t out = (size_t)(y + r) * W + x;
-    const float4 b4 = *reinterpret_cast<const float4*>(b + i);
-    const float4 d4 = *reinterpret_cast<const float4*>(d + i);
-    t[r][0] = make_float4(b4.x, 0.3f, 0.3f, d4.x);
-    t[r][1] = make_float4(b4.y, 0.3f, 0.3f, d4.y);
-    t[r][2] = make_float4(b4.z, 0.3f, 0.3f, d4.z);
-    t[r][3] = make_float4(b4.w, 0.3f, 0.3f, d4.w);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) rgba[out + k] = t[r][k];
-    if (flowmap) {
-      const float4 v01 = *reinterpret_cast<const float4*>(v + i);
-      const float4 v23 = *reinterpret_cast<const float4*>(v + i + 2);
-      const __half2 h0 = __floats2half2_rn(v01.x, v01.y), h1 = __floats2half2_rn(v01.z, v01.w);
-      const __half2 h2 = __floats2half2_rn(v23.x, v23.y), h3 = __floats2half2_rn(v23.z, v23.w);
-      uint4 packed;
-      packed.x = *reinterpret_cast<const uint32_t*>(&h0);
-      packed.y = *reinterpret_cast<const uint32_t*>(&h1);
-      packed.z = *reinterpret_cast<const uint32_t*>(&h2);
-      packed.w = *reinterpret_cast<const uint32_t*>(&h3);
-      *reinterpret_cast<uint4*>(flowmap + out) = packed;
-    }
-  }
-  // level 1 texel (x/2 + j, y/2) from cells (x + 2j, y), (x + 2j + 1, y),
-  // (x + 2j, y + 1), (x + 2j + 1, y + 1), in the order of mip_chain_kernel's filter
-  const size_t m = (size_t)(y / 2) * (W / 2) + x / 2;
-#pragma unroll
-  for (int j = 0; j < 2; ++j) {
-    const float4 a = t[0][2 * j], c0 = t[0][2 * j + 1], c = t[1][2 * j], e = t[1][2 * j + 1];
-    mip1[m + j] = make_float4(avg4(a.x, c0.x, c.x, e.x), avg4(a.y, c0.y, c.y, e.y),
-                              avg4(a.z, c0.z, c.z, e.z), avg4(a.w, c0.w, c.w, e.w));
-  }
-}
-
 __global__ void terrain_rgba_kernel(const float* __restrict__ b, const float* __restrict__ d,
                                     int W, int H, int pitch, float4* __restrict__ out) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -301,9 +252,12 @@ __global__ void __launch_bounds__(256)
     if (gx < c.w[0] && gy < c.h[0]) c.dst[0][(size_t)gy * c.w[0] + gx] = r;
   }
   __syncthreads();
-  int side = Q;
-  for (int l = 1; l < c.n; ++l) {
-    const int half = side / 2;
+  // unrolled so that every level index is a constant (an indexed kernel
+  // parameter would be copied to local memory)
+#pragma unroll
+  for (int l = 1; l < kMipChain; ++l) {
+    if (l >= c.n) break;  // the same for every thread
+    const int side = Q >> (l - 1), half = side / 2;
     const float4* in = buf[(l - 1) & 1];
     float4* out = buf[l & 1];
     const int ox = bx >> (l + 1), oy = by >> (l + 1);  // the block's origin in this level
@@ -318,7 +272,101 @@ __global__ void __launch_bounds__(256)
       if (gx < c.w[l] && gy < c.h[l]) c.dst[l][(size_t)gy * c.w[l] + gx] = r;
     }
     __syncthreads();
-    side = half;
+  }
+}
+
+// export_kernel4's work for a 64 x 64 block of cells (W % 4 == 0, H even)
+// plus up to six mip levels of the block (32 x 32 texels down to 1 x 1): each
+// thread exports two 4 x 2 patches and filters each into two level-1 texels
+// in registers, and the CTA halves level 1 in shared memory down to the last
+// level, with the filter of mip_chain_kernel.  Texels past a level's edge are
+// computed from zero fill and not written; level-1 texels inside the level
+// use only cells on the grid.
+constexpr int kMipFused = 6;  // 64 -> 32 -> 16 -> 8 -> 4 -> 2 -> 1
+struct MipLevels {
+  float4* dst[kMipFused];
+  int w[kMipFused], h[kMipFused];  // sizes of the levels written
+  int n;                           // levels written, 1 .. kMipFused
+};
+
+__global__ void __launch_bounds__(256)
+    export_mips_kernel4(const float* __restrict__ b, const float* __restrict__ d,
+                        const float2* __restrict__ v, int W, int H, int pitch,
+                        float4* __restrict__ rgba, __half2* __restrict__ flowmap, MipLevels m) {
+  constexpr int Q = 32;  // level-1 texels per block side
+  __shared__ float4 buf[2][Q * Q];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;  // 16 x 16 threads
+  const int bx = blockIdx.x * 64, by = blockIdx.y * 64;
+  const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int half = 0; half < 2; ++half) {
+    // cells (x .. x + 3, y .. y + 1); level-1 texels (x/2, x/2 + 1) of row y/2
+    const int x = bx + 4 * tx, y = by + 4 * ty + 2 * half;
+    float4 t[2][4];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      if (x < W && y + r < H) {
+        const size_t i = (size_t)(y + r) * pitch + x;
+        const size_t out = (size_t)(y + r) * W + x;
+        const float4 b4 = *reinterpret_cast<const float4*>(b + i);
+        const float4 d4 = *reinterpret_cast<const float4*>(d + i);
+        t[r][0] = make_float4(b4.x, 0.3f, 0.3f, d4.x);
+        t[r][1] = make_float4(b4.y, 0.3f, 0.3f, d4.y);
+        t[r][2] = make_float4(b4.z, 0.3f, 0.3f, d4.z);
+        t[r][3] = make_float4(b4.w, 0.3f, 0.3f, d4.w);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) rgba[out + k] = t[r][k];
+        if (flowmap) {
+          const float4 v01 = *reinterpret_cast<const float4*>(v + i);
+          const float4 v23 = *reinterpret_cast<const float4*>(v + i + 2);
+          const __half2 h0 = __floats2half2_rn(v01.x, v01.y);
+          const __half2 h1 = __floats2half2_rn(v01.z, v01.w);
+          const __half2 h2 = __floats2half2_rn(v23.x, v23.y);
+          const __half2 h3 = __floats2half2_rn(v23.z, v23.w);
+          uint4 packed;
+          packed.x = *reinterpret_cast<const uint32_t*>(&h0);
+          packed.y = *reinterpret_cast<const uint32_t*>(&h1);
+          packed.z = *reinterpret_cast<const uint32_t*>(&h2);
+          packed.w = *reinterpret_cast<const uint32_t*>(&h3);
+          *reinterpret_cast<uint4*>(flowmap + out) = packed;
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) t[r][k] = z;
+      }
+    }
+    const int qy = 2 * ty + half, gy = (by >> 1) + qy;
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const float4 a = t[0][2 * j], c0 = t[0][2 * j + 1], c = t[1][2 * j], e = t[1][2 * j + 1];
+      const float4 r = make_float4(avg4(a.x, c0.x, c.x, e.x), avg4(a.y, c0.y, c.y, e.y),
+                                   avg4(a.z, c0.z, c.z, e.z), avg4(a.w, c0.w, c.w, e.w));
+      const int qx = 2 * tx + j, gx = (bx >> 1) + qx;
+      buf[0][qy * Q + qx] = r;
+      if (gx < m.w[0] && gy < m.h[0]) m.dst[0][(size_t)gy * m.w[0] + gx] = r;
+    }
+  }
+  __syncthreads();
+  // levels 2 .. m.n, unrolled so that every level index is a constant (an
+  // indexed kernel parameter would be copied to local memory)
+#pragma unroll
+  for (int l = 1; l < kMipFused; ++l) {
+    if (l >= m.n) break;  // the same for every thread
+    const int side = Q >> (l - 1), half = side / 2;
+    const float4* in = buf[(l - 1) & 1];
+    float4* out = buf[l & 1];
+    const int ox = bx >> (l + 1), oy = by >> (l + 1);  // the block's origin in this level
+    for (int i = threadIdx.x; i < half * half; i += blockDim.x) {
+      const int x = i % half, y = i / half;
+      const float4 a = in[(2 * y) * side + 2 * x], c0 = in[(2 * y) * side + 2 * x + 1];
+      const float4 c = in[(2 * y + 1) * side + 2 * x], e = in[(2 * y + 1) * side + 2 * x + 1];
+      const float4 r = make_float4(avg4(a.x, c0.x, c.x, e.x), avg4(a.y, c0.y, c.y, e.y),
+                                   avg4(a.z, c0.z, c.z, e.z), avg4(a.w, c0.w, c.w, e.w));
+      out[y * half + x] = r;
+      const int gx = ox + x, gy = oy + y;
+      if (gx < m.w[l] && gy < m.h[l]) m.dst[l][(size_t)gy * m.w[l] + gx] = r;
+    }
+    __syncthreads();
   }
 }
 
@@ -352,10 +400,23 @@ cudaError_t launch_export(const float* b, const float* d, const float2* v, int W
   const bool wide = W % 4 == 0 && aligned(terrain_rgba, 16) && aligned(flowmap, 16);
   // with mips, the first level comes out of the same pass (even heights)
   const bool fuse_mip1 = wide && terrain_rgba && mips && mip_levels >= 1 && H % 2 == 0;
+  MipLevels fused{};
   if (fuse_mip1) {
-    export_mip1_kernel4<<<grid2d(W / 4, H / 2), dim3(32, 8), 0, s>>>(
+    // the export and up to six mip levels in one pass
+    float4* p = reinterpret_cast<float4*>(mips);
+    int w = W, h = H;
+    while (fused.n < kMipFused && fused.n < mip_levels && w >= 2 && h >= 2) {
+      w /= 2;
+      h /= 2;
+      fused.dst[fused.n] = p;
+      fused.w[fused.n] = w;
+      fused.h[fused.n] = h;
+      p += (size_t)w * h;
+      ++fused.n;
+    }
+    export_mips_kernel4<<<dim3((W + 63) / 64, (H + 63) / 64), 256, 0, s>>>(
         b, d, v, W, H, pitch, reinterpret_cast<float4*>(terrain_rgba),
-        reinterpret_cast<__half2*>(flowmap), reinterpret_cast<float4*>(mips));
+        reinterpret_cast<__half2*>(flowmap), fused);
     count_launch();
   } else if (wide && (flowmap || terrain_rgba)) {
     export_kernel4<<<grid2d(W / 4, H), dim3(32, 8), 0, s>>>(
@@ -378,15 +439,15 @@ cudaError_t launch_export(const float* b, const float* d, const float2* v, int W
     const float4* src = reinterpret_cast<const float4*>(terrain_rgba);
     float4* dst = reinterpret_cast<float4*>(mips);
     int sw = W, sh = H, l = 1;
-    if (fuse_mip1) {  // level 1 is written; continue from it
-      src = dst;
-      dst += (size_t)(W / 2) * (H / 2);
-      sw = W / 2;
-      sh = H / 2;
-      l = 2;
+    if (fuse_mip1) {  // levels 1 .. fused.n are written; continue from the last
+      src = fused.dst[fused.n - 1];
+      dst = fused.dst[fused.n - 1] + (size_t)fused.w[fused.n - 1] * fused.h[fused.n - 1];
+      sw = fused.w[fused.n - 1];
+      sh = fused.h[fused.n - 1];
+      l = fused.n + 1;
     }
-    // the remaining levels, up to kMipChain per launch (4096^2: 3 launches
-    // for levels 2..12 instead of 11)
+    // the remaining levels, up to kMipChain per launch (4096^2: 2 launches
+    // for levels 7..12)
     while (l <= mip_levels && sw >= 2 && sh >= 2) {
       MipChain c{};
       int w = sw, h = sh;

@@ -80,7 +80,8 @@ def test_surface_matches_reference_render_fixture(tws):
     assert np.array_equal(got["dry"], g0["out_dry"])
 
 
-@pytest.mark.parametrize("W,H,levels", [(64, 48, 3), (100, 37, 2), (38, 21, 2), (256, 256, 8)])
+@pytest.mark.parametrize("W,H,levels", [(64, 48, 3), (100, 37, 2), (38, 21, 2), (256, 256, 8),
+                                          (200, 136, 7), (640, 382, 8)])
 def test_texture_export_matches_oracle(tws, oracle, W, H, levels):
     import torch
     with tws.Grid(W, H) as g:
